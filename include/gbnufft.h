@@ -1,0 +1,167 @@
+/* gbnufft.h -- C ABI of the GB300 table-mode NUFFT (libgbnufft.so).
+ *
+ * Plain C types only: host pointers, device pointers (void*), sizes, a CUDA
+ * stream passed as void* (0 = legacy default stream).  Every entry point
+ * returns a status code (GBN_OK on success); gbn_last_error() describes the
+ * most recent failure on the calling thread.  No entry point aborts.
+ *
+ * Axis convention.  The plan is described in MEMORY-AXIS order: axis 0 is
+ * the fastest-varying index of the image and of the oversampled grid.  A
+ * Fortran-ordered numpy image of shape Nd (the reference's layout,
+ * mrrt/nufft/_nufft.py:1306) maps omega column d to memory axis d; a
+ * C-ordered [batch, N0, N1] tensor maps omega column d to memory axis
+ * ndim-1-d.  The Python layer performs that mapping.
+ *
+ * Data layouts (complex values are interleaved re/im, complex64 for single
+ * precision, complex128 for double):
+ *   image   x : [frames][coils][N_{ndim-1}]...[N_0]
+ *   grid      : [frames][coils][K_{ndim-1}]...[K_0]
+ *   samples y : frame f occupies [coils][M_f] starting at
+ *               coils * frame_offsets[f]
+ *   tm        : host, [M_total][ndim] with column d = coordinate on memory
+ *               axis d, in units of oversampled-grid cells (omega / (2 pi / K)),
+ *               the reference's tm (mrrt/nufft/_nufft.py:338-342).
+ */
+#ifndef GBNUFFT_H
+#define GBNUFFT_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GBN_OK 0
+#define GBN_ERR_INVALID 1     /* bad argument (shape, size, pointer, flag)   */
+#define GBN_ERR_CUDA 2        /* CUDA runtime error                           */
+#define GBN_ERR_CUFFT 3       /* cuFFT error                                  */
+#define GBN_ERR_NOMEM 4       /* device or host allocation failed             */
+#define GBN_ERR_UNSUPPORTED 5 /* valid request outside what is implemented    */
+#define GBN_ERR_TOOLARGE 6    /* request exceeds a fixed capacity             */
+
+#define GBN_PRECISION_SINGLE 0
+#define GBN_PRECISION_DOUBLE 1
+#define GBN_PHASING_REAL 0
+#define GBN_PHASING_COMPLEX 1
+
+/* Geometry of one operator (or of a series of frames sharing it). */
+typedef struct gbn_geometry {
+    int ndim;              /* 1, 2 or 3                                       */
+    int Nd[3];             /* image size per memory axis                      */
+    int Kd[3];             /* oversampled grid size per memory axis           */
+    int Jd[3];             /* kernel width per memory axis (1..8)             */
+    int L;                 /* table samples per grid unit                     */
+    int precision;         /* GBN_PRECISION_*                                 */
+    int phasing;           /* GBN_PHASING_*                                   */
+    int ortho;             /* 1: orthonormal FFT scaling                      */
+    double adjoint_scale;  /* adjoint_scalefactor                             */
+    /* real phasing: phase_before(k) = exp(i * sum_d c_d k_d), the per-axis
+     * coefficient c_d = 2 pi n_mid_d / K_d; the partial sums are rounded in
+     * the working precision in the order given by pb_order (reference axis
+     * order, mrrt/nufft/_nufft.py:703-715).                                  */
+    double pb_coef[3];
+    int pb_order[3];
+    int n_frames;          /* number of sample sets (1 for a plain operator) */
+    int tile[3];           /* tile edge per memory axis, 0 = default          */
+    int max_coils;         /* largest coil count a call will use              */
+    int flags;             /* reserved, 0                                     */
+} gbn_geometry;
+
+typedef struct gbn_plan gbn_plan;
+
+/* Create a plan.  Replaces the reference's per-operator set-up
+ * (NufftBase.__init__ table branch, mrrt/nufft/_nufft.py:216-390).
+ *   h_re[d], h_im[d] : host lookup tables of length Jd[d]*L+1 for memory axis d
+ *                      (h_im NULL or all-NULL for phasing real).
+ *   sn               : host deapodisation [N_{ndim-1}]...[N_0] (real).
+ *   frame_offsets    : host [n_frames+1] sample offsets (frame_offsets[0] = 0).
+ *   tm               : host [M_total][ndim] coordinates (see header note).
+ *   sample_phase     : host [M_total] complex, applied after interpolation and
+ *                      conjugated before spreading (phase_after for real
+ *                      phasing, phase_shift for complex phasing); may be NULL.
+ * Table, tm and phase arrays are in the plan precision (float or double).    */
+int gbn_plan_create(gbn_plan** plan, const gbn_geometry* geom,
+                    const void* const* h_re, const void* const* h_im,
+                    const void* sn, const int64_t* frame_offsets,
+                    const void* tm, const void* sample_phase, int device);
+
+/* Replace the sample coordinates (and sample phase) of an existing plan with
+ * the same frame offsets; rebuilds the tile lists.                          */
+int gbn_plan_set_points(gbn_plan* plan, const void* tm,
+                        const void* sample_phase);
+
+int gbn_plan_destroy(gbn_plan* plan);
+
+/* Forward NUFFT, image -> samples, `coils` coils per frame.
+ * Replaces nufft_forward (mrrt/nufft/_nufft.py:1275-1397) in table mode:
+ * deapodise + zero-pad, Kd-point FFT, phase_before, table interpolation
+ * (interp{1,2,3}_table, mrrt/nufft/_interp_table.py:26-159, C kernels
+ * {float,double}_interp{1,2,3}_table1_{real,complex}_forward,
+ * mrrt/nufft/_extensions/c/nufft_table.template.h:98-342), sample phase.   */
+int gbn_forward(gbn_plan* plan, const void* x, void* y, int coils,
+                void* stream);
+
+/* Adjoint NUFFT, samples -> image.  Replaces nufft_adj
+ * (mrrt/nufft/_nufft.py:1459-1578) in table mode, including the adjoint
+ * spread interp{1,2,3}_table_adj (C kernels *_adj in the same header).     */
+int gbn_adjoint(gbn_plan* plan, const void* y, void* x, int coils,
+                void* stream);
+
+/* Table interpolation alone: oversampled grid -> samples, no phases, no FFT.
+ * Replaces interp{1,2,3}_table (mrrt/nufft/_interp_table.py:26-159).        */
+int gbn_interp_forward(gbn_plan* plan, const void* grid, void* y, int coils,
+                       void* stream);
+
+/* Adjoint table interpolation alone: samples -> oversampled grid.  Replaces
+ * interp{1,2,3}_table_adj (mrrt/nufft/_interp_table.py:46-191).            */
+int gbn_interp_adjoint(gbn_plan* plan, const void* y, void* grid, int coils,
+                       void* stream);
+
+/* Upload derivative tables dh/dt (host, length Jd[d]*L+1 per memory axis, plan
+ * precision) used by gbn_grad_tm.  No counterpart in the reference.          */
+int gbn_plan_set_dtables(gbn_plan* plan, const void* const* dtab);
+
+/* Gradient of a real loss with respect to the sample coordinates tm
+ * (single-frame plans, real phasing).
+ *   grid : [coils][K...] the forward's oversampled grid before phase_before,
+ *          i.e. the FFT output a gbn_forward call leaves in the buffer that
+ *          gbn_forward_grid returns (callers copy it if they need it later).
+ *   gy   : [coils][M] dL/dy in torch's convention (dL/dRe + i dL/dIm).
+ *   phase_shift : host [ndim], d(sample phase)/d(tm_d) divided by i, i.e.
+ *          (n_shift_d - n_mid_d) * 2 pi / Kd[d] for phase_after.
+ *   gtm  : out, [M][ndim] dL/dtm (plan precision), summed over coils.
+ * No counterpart in the reference (it has no autograd).                     */
+int gbn_grad_tm(gbn_plan* plan, const void* grid, const void* gy,
+                const double* phase_shift, void* gtm, int coils, void* stream);
+
+/* Device pointer of the plan's forward grid buffer (valid until the next
+ * call on the plan).                                                         */
+int gbn_forward_grid(gbn_plan* plan, void** grid);
+
+/* Exact direct NUDFT in double precision on the GPU (the reference's
+ * dtft / dtft_adj, mrrt/nufft/_dtft.py:16-216).
+ *   omega : device [M][ndim] (double), column d pairs with memory axis d.
+ *   x     : device [reps][N_{ndim-1}]...[N_0] complex128.
+ *   y     : device [reps][M] complex128.                                     */
+int gbn_dtft_forward(int ndim, const int* Nd, const double* n_shift,
+                     const void* omega, int64_t M, const void* x, void* y,
+                     int reps, void* stream);
+int gbn_dtft_adjoint(int ndim, const int* Nd, const double* n_shift,
+                     const void* omega, int64_t M, const void* y, void* x,
+                     int reps, void* stream);
+
+/* Plan statistics: 8 int64 values (gather items, spread items, split tiles,
+ * gather list length, spread list length, tiles, device bytes held, M_total). */
+int gbn_plan_stats(const gbn_plan* plan, int64_t* out8);
+
+/* Message of the last failure on the calling thread ("" if none). */
+const char* gbn_last_error(void);
+
+/* Library version string. */
+const char* gbn_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GBNUFFT_H */

@@ -1,0 +1,345 @@
+"""``NufftBase``: drop-in for the reference operator, running on the GB300.
+
+Same constructor signature, ``.fft()`` / ``.adj()`` methods and attributes
+as the reference (mrrt/nufft/_nufft.py:122-621).  Plan-time math (kernel
+shape, deapodisation ``sn``, tables ``h``, normalised coordinates ``tm`` and
+``phase_after``) is computed on the host exactly as the reference computes it
+(same formulas, same numpy dtypes, so the float32 rounding of the phases
+follows the reference); the transforms run in libgbnufft's CUDA kernels.
+There is no CPU execution path.
+
+Input and output conventions follow the reference (mrrt/nufft/_nufft.py:
+1275-1397, 1459-1578): images are ``Nd + (reps,)`` in Fortran order
+(``order='F'``) or ``(reps,) + Nd`` (``order='C'``); sample arrays are
+``(M, reps)`` / ``(reps, M)``; a single repetition is squeezed; real input is
+promoted to the operator's complex dtype and the output dtype always equals
+the operator precision.  ``on_gpu=False`` returns numpy arrays (host buffers,
+copies inside the call); ``on_gpu=True`` returns torch CUDA tensors.  Inputs
+may be numpy arrays or torch tensors in either case.
+"""
+import math
+import warnings
+
+import numpy as np
+import torch
+
+from ._kaiser_bessel import kaiser_bessel_ft
+from ._kernels import BeattyKernel, kernel_deriv_table, kernel_table
+from ._plan import GpuPlan, require_cuda
+
+__all__ = ["NufftBase"]
+
+supported_real_types = [np.float32, np.float64]
+
+
+def _as_tuple(seq, type=int, n=None):
+    if np.isscalar(seq):
+        if n is None:
+            raise ValueError("for scalar, seq, n must be specified")
+        return (type(seq),) * n
+    if n is not None and len(seq) != n:
+        raise ValueError("array did not have the expected size of {}".format(n))
+    return tuple(type(s) for s in seq)
+
+
+def _to_numpy(a):
+    if isinstance(a, torch.Tensor):
+        return a.detach().cpu().numpy()
+    return np.asarray(a)
+
+
+class NufftBase(object):
+    """Non-uniform FFT operator (table-based interpolation) on the GPU.
+
+    Parameters are those of the reference ``NufftBase``; see the module
+    docstring for the data conventions.  ``mode`` must be ``'table'``.
+
+    Extra keyword (not in the reference): ``max_coils`` -- the repetition
+    count the tile plan is sized for (default 1; larger batches re-tile once
+    automatically).
+    """
+
+    def __init__(self, Nd, omega, Jd=4, Kd=None, precision="single", mode="table", Ld=1024,
+                 ortho=False, n_shift=None, phasing="real", adjoint_scalefactor=1.0,
+                 preplan_cufft=True, order="F", verbose=False, on_gpu=False, max_coils=1):
+        require_cuda()
+        self.verbose = verbose
+        self.order = order
+        if order not in ("F", "C"):
+            raise ValueError("order must be 'F' or 'C'")
+        self.on_gpu = on_gpu
+        if np.isscalar(Nd):
+            Nd = (Nd,)
+        self.__Nd = _as_tuple(Nd, type=int)
+        self.ndim = len(self.__Nd)
+        if self.ndim > 3:
+            raise NotImplementedError("dimensions > 3 not implemented")
+        if phasing not in ("real", "complex"):
+            raise ValueError("Invalid phasing: {}. phasing must be 'real' or 'complex'".format(phasing))
+        self.__phasing = phasing
+        self.__Jd = _as_tuple(Jd, type=int, n=self.ndim)
+        if Kd is None:
+            Kd = tuple(int(1.5 * n) for n in self.__Nd)
+        self.__Kd = _as_tuple(Kd, type=int, n=self.ndim)
+        self.ortho = ortho
+        self.scale_ortho = math.sqrt(math.prod(self.__Kd)) if ortho else 1
+        if mode != "table":
+            if mode == "sparse":
+                raise NotImplementedError(
+                    "mode='sparse' is not provided by the GPU operator; use mode='table'")
+            raise ValueError("Invalid NUFFT mode: {}".format(mode))
+        self.__mode = mode
+        self.adjoint_scalefactor = adjoint_scalefactor
+        self.preplan_cufft = preplan_cufft
+        self.p = None
+        self.__Ld = int(Ld)
+        if self.__Ld % 2 == 1 and any(j % 2 == 1 for j in self.__Jd):
+            warnings.warn("accuracy may be compromised when L and J are both odd")
+
+        # omega validation (mrrt/nufft/_nufft.py:552-573)
+        omega = _to_numpy(omega)
+        if omega.ndim == 1:
+            omega = omega[:, np.newaxis]
+        if omega.shape[1] != self.ndim:
+            raise ValueError("number of cols must match NUFFT dimension")
+        if omega.dtype not in supported_real_types:
+            raise ValueError("omega must be one of the following types: {}".format(supported_real_types))
+        if precision == "auto":
+            precision = "single" if omega.dtype == np.float32 else "double"
+        if precision == "single":
+            self._cplx_dtype, self._real_dtype = np.dtype(np.complex64), np.dtype(np.float32)
+        elif precision == "double":
+            self._cplx_dtype, self._real_dtype = np.dtype(np.complex128), np.dtype(np.float64)
+        else:
+            raise ValueError("precision must be 'single', 'double' or 'auto'")
+        self.__precision = precision
+
+        if n_shift is None:
+            self.__n_shift = (0.0,) * self.ndim
+        else:
+            self.__n_shift = _as_tuple(n_shift, type=float, n=self.ndim)
+        if phasing == "real":
+            self.n_mid = tuple(n // 2 for n in self.__Nd)
+        else:
+            self.n_mid = tuple((n - 1) / 2.0 for n in self.__Nd)
+
+        self.kernel = BeattyKernel(shape=self.__Jd, grid_shape=self.__Nd, os_grid_shape=self.__Kd)
+        rdt, cdt = self._real_dtype, self._cplx_dtype
+        # deapodisation: float64 outer product, then the operator dtype
+        sn = np.array([1.0])
+        for d in range(self.ndim):
+            nc = np.arange(-self.n_mid[d], -self.n_mid[d] + self.__Nd[d])
+            tmp = 1 / kaiser_bessel_ft(nc / self.__Kd[d], self.__Jd[d], self.kernel.alpha[d], 0, 1)
+            sn = np.outer(sn.ravel(), tmp.conj())
+        self.sn = np.asfortranarray(sn.reshape(self.__Nd).astype(rdt))
+        # per-sample phase (mrrt/nufft/_nufft.py:717-724, 898-903): omega in its
+        # given dtype, the shift vector in the operator's real dtype
+        if phasing == "real":
+            shift_vec = [(s - m) for s, m in zip(self.__n_shift, self.n_mid)]
+            self.phase_after = np.exp(1j * np.dot(omega, np.asarray(shift_vec, dtype=rdt))).astype(cdt, copy=False)
+            self.phase_shift = None
+            sample_phase = self.phase_after
+        else:
+            self.phase_after = None
+            if any(s != 0 for s in self.__n_shift):
+                self.phase_shift = np.exp(1j * np.dot(omega.astype(rdt), np.asarray(self.__n_shift))).astype(cdt)
+            else:
+                self.phase_shift = None
+            sample_phase = self.phase_shift
+        self.__omega = np.asfortranarray(omega.astype(rdt))
+        self.M = self.__omega.shape[0]
+        tm = np.zeros_like(self.__omega)
+        for d in range(self.ndim):
+            gam = 2 * np.pi / self.__Kd[d]
+            tm[:, d] = self.__omega[:, d] / gam
+        self.tm = tm
+        tdt = cdt if phasing == "complex" else rdt
+        self.h = [kernel_table(self.__Nd[d], self.__Jd[d], self.__Kd[d], self.__Ld, phasing, tdt)
+                  for d in range(self.ndim)]
+        self.nargin1 = math.prod(self.__Nd)
+        self.nargout1 = self.M
+        self._phase_before = None
+        # phase_before(k) = exp(i sum_d c_d k_d), c_d = 2 pi n_mid_d / K_d
+        pb_coef = [2 * np.pi / self.__Kd[d] * self.n_mid[d] for d in range(self.ndim)]
+        self._plan = GpuPlan(
+            self.__Nd, self.__Kd, self.__Jd, self.__Ld, rdt,
+            [np.real(h) for h in self.h],
+            [np.imag(h) for h in self.h] if phasing == "complex" else None,
+            self.sn.ravel(order="F"), np.ascontiguousarray(tm), sample_phase,
+            ortho=ortho, adjoint_scale=adjoint_scalefactor, pb_coef=pb_coef,
+            pb_order=list(range(self.ndim)), phasing=phasing, max_coils=max_coils)
+
+    # ------------------------------------------------------------------ props
+    @property
+    def Nd(self):
+        return self.__Nd
+
+    @property
+    def Kd(self):
+        return self.__Kd
+
+    @property
+    def Jd(self):
+        return self.__Jd
+
+    @property
+    def Ld(self):
+        return self.__Ld
+
+    @property
+    def mode(self):
+        return self.__mode
+
+    @property
+    def phasing(self):
+        return self.__phasing
+
+    @property
+    def precision(self):
+        return self.__precision
+
+    @property
+    def n_shift(self):
+        return self.__n_shift
+
+    @property
+    def omega(self):
+        return self.__omega
+
+    @property
+    def xp(self):
+        return torch if self.on_gpu else np
+
+    @property
+    def plan(self):
+        """The underlying :class:`GpuPlan` (memory-axis order = reference axis order)."""
+        return self._plan
+
+    @property
+    def phase_before(self):
+        """Kd-grid phase exp(i sum_d 2 pi n_mid_d k_d / K_d) as the reference
+        builds it (mrrt/nufft/_nufft.py:703-715); computed on first access."""
+        if self.__phasing != "real":
+            return None
+        if self._phase_before is None:
+            rdt = self._real_dtype
+            ph = (2 * np.pi / self.__Kd[0] * self.n_mid[0]) * np.arange(self.__Kd[0], dtype=rdt)
+            for d in range(1, self.ndim):
+                tmp = (2 * np.pi / self.__Kd[d] * self.n_mid[d]) * np.arange(self.__Kd[d], dtype=rdt)
+                ph = ph.reshape(ph.shape + (1,)) + tmp.reshape((1,) * d + (tmp.size,))
+            self._phase_before = np.exp(1j * ph).astype(self._cplx_dtype, copy=False)
+        return self._phase_before
+
+    def kernel_deriv_tables(self):
+        """Derivative tables dh/dt per axis (phasing 'real'), for the trajectory gradient."""
+        return [kernel_deriv_table(self.__Nd[d], self.__Jd[d], self.__Kd[d], self.__Ld, self._real_dtype)
+                for d in range(self.ndim)]
+
+    # ------------------------------------------------------------- transforms
+    def _device_in(self, a, narg, leading_shape):
+        """Return (tensor [reps, *reversed(leading_shape)] contiguous on the
+        plan device, reps).  ``a`` follows the Fortran-order convention
+        leading_shape + (reps,)."""
+        dev = self._plan.device
+        ct = self._plan.ctype
+        if isinstance(a, torch.Tensor):
+            t = a.detach()
+            if not t.is_complex():
+                t = t.to(torch.float64 if self._real_dtype == np.float64 else torch.float32)
+            t = t.to(device=dev, dtype=ct)
+        else:
+            arr = np.asarray(a)
+            if arr.dtype != self._cplx_dtype:
+                arr = arr.astype(self._cplx_dtype)
+            t = None
+        total = (t.numel() if t is not None else arr.size)
+        if total % narg != 0:
+            raise ValueError("Input signal has the wrong size.")
+        reps = total // narg
+        full = tuple(leading_shape) + (reps,)
+        if t is not None:
+            t = t.reshape(full) if t.dim() != len(full) or tuple(t.shape) != full else t
+            t = t.permute(*reversed(range(len(full)))).contiguous()
+        else:
+            arr = np.asfortranarray(arr.reshape(full, order="F") if arr.shape != full else arr)
+            host = torch.from_numpy(arr.ravel(order="F"))
+            if torch.cuda.is_available():
+                host = host.pin_memory()
+            t = host.to(dev, non_blocking=True).reshape(tuple(reversed(full)))
+        return t, reps
+
+    def _device_out(self, t, reps, leading_shape):
+        """Convert a device tensor [reps, *reversed(leading_shape)] to the
+        Fortran-order result leading_shape + (reps,) (squeezed for reps == 1)."""
+        nd = len(leading_shape) + 1
+        if self.on_gpu:
+            out = t.permute(*reversed(range(nd)))
+        else:
+            out = t.cpu().numpy().transpose(tuple(reversed(range(nd))))
+        if reps == 1:
+            out = out[..., 0]
+        return out
+
+    def _swap_reps(self, x, narg):
+        size = x.numel() if isinstance(x, torch.Tensor) else np.size(x)
+        if size != narg:
+            nd = x.dim() if isinstance(x, torch.Tensor) else np.ndim(x)
+            perm = tuple(range(1, nd)) + (0,)
+            x = x.permute(*perm) if isinstance(x, torch.Tensor) else np.transpose(x, perm)
+        return x
+
+    def _unswap_reps(self, x, narg):
+        size = x.numel() if isinstance(x, torch.Tensor) else np.size(x)
+        if size != narg:
+            nd = x.dim() if isinstance(x, torch.Tensor) else np.ndim(x)
+            perm = (nd - 1,) + tuple(range(nd - 1))
+            x = x.permute(*perm) if isinstance(x, torch.Tensor) else np.transpose(x, perm)
+        return x
+
+    def fft(self, x):
+        """Forward NUFFT (uniform image -> non-uniform samples)."""
+        if self.order == "C":
+            x = self._swap_reps(x, self.nargin1)
+        xt, reps = self._device_in(x, self.nargin1, self.__Nd)
+        y = torch.empty((reps, self.M), dtype=self._plan.ctype, device=self._plan.device)
+        self._plan.forward(xt, y, reps)
+        out = self._device_out(y, reps, (self.M,))
+        if self.order == "C":
+            out = self._unswap_reps(out, self.nargout1)
+        return out
+
+    def adj(self, k):
+        """Adjoint NUFFT (non-uniform samples -> uniform image)."""
+        if self.order == "C":
+            k = self._swap_reps(k, self.nargout1)
+        yt, reps = self._device_in(k, self.M, (self.M,))
+        x = torch.empty((reps,) + tuple(reversed(self.__Nd)), dtype=self._plan.ctype,
+                        device=self._plan.device)
+        self._plan.adjoint(yt, x, reps)
+        out = self._device_out(x, reps, self.__Nd)
+        if self.order == "C":
+            out = self._unswap_reps(out, self.nargin1)
+        return out
+
+    # ------------------------------------------- table interpolation alone
+    def interp_table(self, xk):
+        """Table interpolation only (the reference's ``_nufft_table_interp``
+        without its phase_shift, mrrt/nufft/_nufft.py:998-1097): oversampled
+        grid ``[prod(Kd), reps]`` (Fortran order) -> samples ``[M, reps]``."""
+        gt, reps = self._device_in(xk, math.prod(self.__Kd), self.__Kd)
+        y = torch.empty((reps, self.M), dtype=self._plan.ctype, device=self._plan.device)
+        self._plan.interp_forward(gt, y, reps)
+        return self._device_out(y, reps, (self.M,))
+
+    def interp_table_adj(self, xm):
+        """Adjoint table interpolation only (``_nufft_table_adj`` without its
+        phase, mrrt/nufft/_nufft.py:1101-1191): samples ``[M, reps]`` ->
+        oversampled grid ``[*Kd, reps]`` (Fortran order)."""
+        yt, reps = self._device_in(xm, self.M, (self.M,))
+        g = torch.empty((reps,) + tuple(reversed(self.__Kd)), dtype=self._plan.ctype,
+                        device=self._plan.device)
+        self._plan.interp_adjoint(yt, g, reps)
+        return self._device_out(g, reps, self.__Kd)
+
+    def __getstate__(self):
+        raise TypeError("NufftBase holds GPU state; rebuild it from (Nd, omega, ...) instead of pickling")

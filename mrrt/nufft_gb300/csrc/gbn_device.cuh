@@ -1,0 +1,135 @@
+// Device helpers shared by the NUFFT kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+
+#include "gbn_internal.h"
+
+namespace gbn {
+
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+    return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ double2 cmul(double2 a, double2 b) {
+    return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+// a * conj(b)
+__device__ __forceinline__ float2 cmulc(float2 a, float2 b) {
+    return make_float2(a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y);
+}
+__device__ __forceinline__ double2 cmulc(double2 a, double2 b) {
+    return make_double2(a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y);
+}
+
+template <typename R> __device__ __forceinline__ typename Cx<R>::T cmake(R re, R im);
+template <> __device__ __forceinline__ float2 cmake<float>(float re, float im) {
+    return make_float2(re, im);
+}
+template <> __device__ __forceinline__ double2 cmake<double>(double re, double im) {
+    return make_double2(re, im);
+}
+
+__device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ void sincos_r(float x, float* s, float* c) { sincosf(x, s, c); }
+__device__ __forceinline__ void sincos_r(double x, double* s, double* c) { sincos(x, s, c); }
+
+// k mod K for k in a few periods around [0, K).
+__device__ __forceinline__ int wrapk(int k, int K) {
+    int r = k % K;
+    return r < 0 ? r + K : r;
+}
+
+// First tap of the window: 1 + floor(t - J/2), evaluated in double exactly as
+// the reference C does (nufft_table.template.c:577-578).
+template <typename R>
+__device__ __forceinline__ int first_tap(R t, int J) {
+    return 1 + (int)floor((double)t - 0.5 * (double)J);
+}
+
+// phase_before(k) = exp(i * sum_d c_d k_d) with every product and partial sum
+// rounded in the working precision, summed in the reference's axis order
+// (mrrt/nufft/_nufft.py:703-715).
+template <typename R>
+__device__ __forceinline__ typename Cx<R>::T phase_before(const Geom<R>& g, const int* k) {
+    R ph[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+        ph[d] = d < g.ndim ? mul_rn(g.pbc[d], (R)k[d]) : (R)0;
+    R s = ph[g.pbo[0]];
+    for (int i = 1; i < g.ndim; ++i) s = add_rn(s, ph[g.pbo[i]]);
+    R sn, cs;
+    sincos_r(s, &sn, &cs);
+    return cmake<R>(cs, sn);
+}
+
+// Linearly interpolated table coefficient for tap k of coordinate t
+// (nufft_table.template.c:581-585):  p = (t - k) L, n = floor(p),
+// coef = (1 - alf) h[n] + alf h[n + 1].  Tables are zero-padded by two
+// entries on each side on the device, so the one-past-the-end read that
+// occurs when t - J/2 is an integer stays in bounds.
+template <typename R, bool CX>
+__device__ __forceinline__ void table_coef(const Geom<R>& g, int d, R t, int k, R& cr, R& ci) {
+    const R pp = (t - (R)k) * (R)g.L;
+    const R nf = floor(pp);
+    const int n = (int)nf + g.ncenter[d];
+    const R alf = pp - nf;
+    const R* h = g.hr[d];
+    cr = ((R)1 - alf) * __ldg(h + n) + alf * __ldg(h + n + 1);
+    if (CX) {
+        const R* hi = g.hi[d];
+        ci = ((R)1 - alf) * __ldg(hi + n) + alf * __ldg(hi + n + 1);
+    } else {
+        ci = (R)0;
+    }
+}
+
+// Tile coordinates of a linear tile index (axis 0 fastest).
+template <int NDIM>
+__device__ __forceinline__ void tile_origin(int tile, const int* nt, const int* T, int* org) {
+    int rem = tile;
+#pragma unroll
+    for (int d = 0; d < NDIM; ++d) {
+        const int tc = rem % nt[d];
+        rem /= nt[d];
+        org[d] = tc * T[d];
+    }
+}
+
+template <typename R>
+__device__ __forceinline__ int region_dims(const Geom<R>& g, int ndim, int* Rd) {
+    int tot = 1;
+    for (int d = 0; d < 3; ++d) {
+        Rd[d] = d < ndim ? g.T[d] + g.J[d] - 1 : 1;
+        tot *= Rd[d];
+    }
+    return tot;
+}
+
+// Complex FMA helpers: acc += c * v with c = (cr, ci) (ci == 0 when !CX).
+template <bool CX, typename C, typename R>
+__device__ __forceinline__ void cfma(C& acc, R cr, R ci, C v) {
+    acc.x += cr * v.x;
+    acc.y += cr * v.y;
+    if (CX) {
+        acc.x -= ci * v.y;
+        acc.y += ci * v.x;
+    }
+}
+// acc += conj(c) * v
+template <bool CX, typename C, typename R>
+__device__ __forceinline__ C cscale_conj(R cr, R ci, C v) {
+    C r;
+    r.x = cr * v.x;
+    r.y = cr * v.y;
+    if (CX) {
+        r.x += ci * v.y;
+        r.y -= ci * v.x;
+    }
+    return r;
+}
+
+}  // namespace gbn

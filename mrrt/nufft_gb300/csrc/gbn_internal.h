@@ -1,0 +1,149 @@
+// Internal declarations shared by the host planner (gbn_plan.cu) and the
+// device kernels (gbn_interp.cu, gbn_padcrop.cu, gbn_grad.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+
+namespace gbn {
+
+// Kernel width limit of the register-resident coefficient arrays.
+constexpr int JMAX = 8;
+
+template <typename R> struct Cx;
+template <> struct Cx<float> { typedef float2 T; };
+template <> struct Cx<double> { typedef double2 T; };
+
+// Geometry in memory-axis order (axis 0 fastest).
+template <typename R>
+struct Geom {
+    int ndim;
+    int N[3], K[3], J[3], T[3], nt[3];
+    int L;
+    int ncenter[3];          // floor(J*L/2): table index of t = 0
+    const R* hr[3];          // device tables (not shifted)
+    const R* hi[3];          // imaginary tables, nullptr for a real kernel
+    int64_t Kprod, Nprod;
+    R pbc[3];                // phase_before coefficient per memory axis
+    int pbo[3];              // summation order of the per-axis phases
+};
+
+// Coil-lane layout of a CTA: LS lanes per sample (power of two <= 32),
+// SW = 32 / LS samples per warp.  Staged grid values for one cell occupy
+// LSP complex slots; for LS == 32 the slot is XOR-swizzled (swz = 31)
+// instead of padded.
+struct Lanes {
+    int LS, lsh, LSP, swz;
+};
+
+// Sorted sample list (one per direction).
+template <typename R>
+struct SampleList {
+    const R* t[3];                  // coordinate per memory axis, list order
+    const int* idx;                 // sample index within its frame
+    const typename Cx<R>::T* ph;    // per-sample phase (list order) or nullptr
+};
+
+template <typename R>
+struct GatherParams {
+    Geom<R> g;
+    Lanes ln;
+    SampleList<R> s;
+    const int4* items;              // {frame, tile, start, count}
+    int nitems;
+    int coils;
+    const int64_t* foff;            // device frame offsets [F+1]
+    const typename Cx<R>::T* grid;  // [F][coils][Kprod]
+    typename Cx<R>::T* y;           // samples
+    int apply_pb;                   // multiply staged cells by phase_before
+    R grid_scale;                   // divide staged cells by this (ortho)
+    int apply_ph;                   // multiply outputs by the sample phase
+};
+
+template <typename R>
+struct SpreadParams {
+    Geom<R> g;
+    Lanes ln;
+    SampleList<R> s;
+    const int4* items;              // {frame, tile, start, count}
+    const int2* parts;              // {scratch slot or -1, nparts}
+    int nitems;
+    int coils;
+    const int64_t* foff;
+    const typename Cx<R>::T* y;
+    typename Cx<R>::T* grid;
+    typename Cx<R>::T* scratch;     // [slot][tile cells][LS] partial sums
+    int64_t tile_cells;             // T0*T1*T2
+    int apply_pb;
+    int apply_ph;
+};
+
+template <typename R>
+struct ReduceParams {
+    Geom<R> g;
+    Lanes ln;
+    const int4* tiles;              // {frame, tile, first slot, nparts}
+    int ntiles;
+    int coils;
+    const typename Cx<R>::T* scratch;
+    typename Cx<R>::T* grid;
+    int64_t tile_cells;
+    int apply_pb;
+};
+
+template <typename R>
+struct PadParams {
+    int ndim;
+    int N[3], K[3];
+    int64_t Nprod, Kprod;
+    int planes;
+    const typename Cx<R>::T* x;
+    const R* sn;
+    typename Cx<R>::T* out;
+};
+
+template <typename R>
+struct CropParams {
+    int ndim;
+    int N[3], K[3];
+    int64_t Nprod, Kprod;
+    int planes;
+    const typename Cx<R>::T* grid;
+    const R* sn;
+    R scale;
+    typename Cx<R>::T* x;
+};
+
+template <typename R>
+struct GradParams {
+    Geom<R> g;
+    const R* t[3];                  // coordinates, gather-list order
+    const int* idx;                 // sample index of each list entry
+    const R* dh[3];                 // derivative tables (shifted by 2 like hr)
+    const typename Cx<R>::T* ph;    // sample phase, list order, or nullptr
+    R phase_shift[3];               // s_d * gamma_d: d(phase)/d(tm_d) / i
+    int64_t M;                      // list length (single frame)
+    int coils;
+    int apply_pb;
+    R grid_scale;
+    const typename Cx<R>::T* grid;  // [coils][Kprod], before phase_before
+    const typename Cx<R>::T* gy;    // [coils][M] incoming gradient
+    R* gtm;                         // [M][ndim] out
+};
+
+template <typename R> cudaError_t launch_gather(const GatherParams<R>& p, cudaStream_t s);
+template <typename R> cudaError_t launch_spread(const SpreadParams<R>& p, cudaStream_t s);
+template <typename R> cudaError_t launch_reduce(const ReduceParams<R>& p, cudaStream_t s);
+template <typename R> cudaError_t launch_pad(const PadParams<R>& p, cudaStream_t s);
+template <typename R> cudaError_t launch_crop(const CropParams<R>& p, cudaStream_t s);
+template <typename R> cudaError_t launch_grad(const GradParams<R>& p, cudaStream_t s);
+
+// Shared-memory bytes needed by the gather / spread kernels for a lane layout.
+template <typename R> size_t gather_smem(const Geom<R>& g, const Lanes& ln);
+template <typename R> size_t spread_smem(const Geom<R>& g, const Lanes& ln);
+
+cudaError_t launch_dtft(bool adjoint, int ndim, const int* Nd, const double* n_shift,
+                        const double* omega, int64_t M, const double2* in, double2* out,
+                        int reps, cudaStream_t s);
+
+}  // namespace gbn

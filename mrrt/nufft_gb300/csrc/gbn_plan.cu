@@ -1,0 +1,876 @@
+// Host side of libgbnufft: plan construction (tile planner), cuFFT plans,
+// device buffers and the C ABI declared in include/gbnufft.h.
+//
+// The plan corresponds to the reference's operator set-up in table mode
+// (mrrt/nufft/_nufft.py:216-390): tables, deapodisation and sample
+// coordinates are uploaded once; in addition the planner sorts samples by
+// grid tile (the reference's GPU path has no such step -- it scatters with
+// global atomics, mrrt/nufft/cuda/jinja/table_2d_adjoint.jinja).
+#include <cuda_runtime.h>
+#include <cufft.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../../include/gbnufft.h"
+#include "gbn_internal.h"
+
+using namespace gbn;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string& msg) {
+    g_last_error = msg;
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char* where) {
+    return fail(GBN_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+int cufft_fail(cufftResult r, const char* where) {
+    return fail(GBN_ERR_CUFFT, std::string(where) + ": cuFFT error " + std::to_string((int)r));
+}
+
+#define GBN_CUDA(call, where)                          \
+    do {                                               \
+        cudaError_t e__ = (call);                      \
+        if (e__ != cudaSuccess) return cuda_fail(e__, where); \
+    } while (0)
+
+int next_pow2(int v) {
+    int p = 1;
+    while (p < v) p <<= 1;
+    return p;
+}
+
+int ilog2(int v) {
+    int l = 0;
+    while ((1 << l) < v) ++l;
+    return l;
+}
+
+// Largest number of coil lanes per sample for a given dimensionality.
+int lane_cap(int ndim) { return ndim >= 3 ? 8 : 32; }
+
+Lanes make_lanes(int ndim, int coils) {
+    Lanes ln;
+    ln.LS = std::min(lane_cap(ndim), next_pow2(std::max(coils, 1)));
+    ln.lsh = ilog2(ln.LS);
+    ln.LSP = ln.LS == 32 ? 32 : (ln.LS == 1 ? 1 : ln.LS + 1);
+    ln.swz = ln.LS == 32 ? 31 : 0;
+    return ln;
+}
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    ~DevBuf() {
+        if (p) cudaFree(p);
+    }
+    cudaError_t alloc(size_t b) {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+        if (b == 0) return cudaSuccess;
+        cudaError_t e = cudaMalloc(&p, b);
+        if (e == cudaSuccess) bytes = b;
+        return e;
+    }
+};
+
+struct FftEntry {
+    int planes;
+    cufftHandle h;
+};
+
+constexpr int GATHER_CHUNK = 512;   // samples per gather work item
+constexpr int SPREAD_CHUNK = 512;   // list entries per spread work item
+constexpr size_t SMEM_BUDGET = 112 * 1024;
+
+}  // namespace
+
+struct gbn_plan {
+    int device = 0;
+    gbn_geometry geom;
+    bool dbl = false;
+    bool cx = false;
+    int F = 1;
+    int64_t M_total = 0;
+    std::vector<int64_t> foff;
+    int T[3] = {1, 1, 1}, nt[3] = {1, 1, 1};
+    int ntiles = 1;       // per frame
+    int64_t Kprod = 1, Nprod = 1;
+    int rsize = 4;        // sizeof(R)
+    bool has_phase = false;
+
+    DevBuf tables, dtables, sn, dfoff;
+    DevBuf glist, gitems;
+    DevBuf slist, sitems, sparts, rtiles;
+    int n_gitems = 0, n_sitems = 0, n_rtiles = 0, n_slots = 0;
+    int64_t glen = 0, slen = 0;
+    DevBuf pad, grid, scratch;
+    int cap_planes = 0;        // planes the pad/grid buffers hold
+    int64_t scratch_cap = 0;   // complex elements
+    std::vector<FftEntry> ffts;
+    std::mutex mu;
+
+    ~gbn_plan() {
+        for (auto& f : ffts) cufftDestroy(f.h);
+    }
+};
+
+namespace {
+
+struct DeviceGuard {
+    int prev = -1;
+    explicit DeviceGuard(int dev) {
+        if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+        if (prev != dev) cudaSetDevice(dev);
+    }
+    ~DeviceGuard() {
+        if (prev >= 0) cudaSetDevice(prev);
+    }
+};
+
+template <typename R>
+Geom<R> make_geom(const gbn_plan* P) {
+    Geom<R> g;
+    std::memset(&g, 0, sizeof(g));
+    const gbn_geometry& G = P->geom;
+    g.ndim = G.ndim;
+    const int64_t tab_stride = 0;
+    (void)tab_stride;
+    const R* base = reinterpret_cast<const R*>(P->tables.p);
+    size_t off = 0;
+    for (int d = 0; d < 3; ++d) {
+        const bool on = d < G.ndim;
+        g.N[d] = on ? G.Nd[d] : 1;
+        g.K[d] = on ? G.Kd[d] : 1;
+        g.J[d] = on ? G.Jd[d] : 1;
+        g.T[d] = P->T[d];
+        g.nt[d] = P->nt[d];
+        g.ncenter[d] = on ? (int)std::floor((double)G.Jd[d] * (double)G.L / 2.0) : 0;
+        g.pbc[d] = on ? (R)G.pb_coef[d] : (R)0;
+        g.pbo[d] = on ? G.pb_order[d] : d;
+        if (on) {
+            const size_t len = (size_t)G.Jd[d] * G.L + 1 + 4;
+            g.hr[d] = base + off + 2;
+            off += len;
+        }
+    }
+    for (int d = 0; d < G.ndim && P->cx; ++d) {
+        const size_t len = (size_t)G.Jd[d] * G.L + 1 + 4;
+        g.hi[d] = base + off + 2;
+        off += len;
+    }
+    g.L = G.L;
+    g.Kprod = P->Kprod;
+    g.Nprod = P->Nprod;
+    return g;
+}
+
+template <typename R>
+SampleList<R> make_list(const gbn_plan* P, const DevBuf& buf, int64_t len) {
+    typedef typename Cx<R>::T C;
+    SampleList<R> s;
+    std::memset(&s, 0, sizeof(s));
+    char* b = reinterpret_cast<char*>(buf.p);
+    size_t off = 0;
+    const int ndim = P->geom.ndim;
+    // layout: ph [len] (if any), t[d] [len] each, idx [len]
+    if (P->has_phase) {
+        s.ph = reinterpret_cast<const C*>(b + off);
+        off += sizeof(C) * (size_t)len;
+    }
+    for (int d = 0; d < ndim; ++d) {
+        s.t[d] = reinterpret_cast<const R*>(b + off);
+        off += sizeof(R) * (size_t)len;
+    }
+    s.idx = reinterpret_cast<const int*>(b + off);
+    return s;
+}
+
+template <typename R>
+size_t list_bytes(const gbn_plan* P, int64_t len) {
+    size_t b = (size_t)len * (sizeof(R) * P->geom.ndim + sizeof(int));
+    if (P->has_phase) b += (size_t)len * sizeof(typename Cx<R>::T);
+    return b + 64;
+}
+
+// Choose tile edges: start from a per-dimension default and halve the
+// largest edge until the gather staging fits the shared-memory budget.
+void choose_tiles(gbn_plan* P) {
+    const gbn_geometry& G = P->geom;
+    const int ndim = G.ndim;
+    const Lanes ln = make_lanes(ndim, G.max_coils);
+    int T[3] = {1, 1, 1};
+    if (ndim == 1) {
+        T[0] = 256;
+    } else if (ndim == 2) {
+        if (ln.LS >= 16) { T[0] = 16; T[1] = 16; }
+        else if (ln.LS >= 4) { T[0] = 32; T[1] = 16; }
+        else { T[0] = 32; T[1] = 32; }
+    } else {
+        if (ln.LS >= 4) { T[0] = 8; T[1] = 8; T[2] = 4; }
+        else { T[0] = 8; T[1] = 8; T[2] = 8; }
+    }
+    for (int d = 0; d < ndim; ++d)
+        if (G.tile[d] > 0) T[d] = G.tile[d];
+    const size_t csz = (size_t)2 * P->rsize;
+    for (int it = 0; it < 32; ++it) {
+        size_t cells = 1;
+        for (int d = 0; d < ndim; ++d) cells *= (size_t)(std::min(T[d], G.Kd[d]) + G.Jd[d] - 1);
+        if (cells * ln.LSP * csz <= SMEM_BUDGET) break;
+        int dm = 0;
+        for (int d = 1; d < ndim; ++d)
+            if (T[d] > T[dm]) dm = d;
+        if (T[dm] <= 1) break;
+        T[dm] /= 2;
+    }
+    for (int d = 0; d < 3; ++d) {
+        P->T[d] = d < ndim ? std::max(1, std::min(T[d], G.Kd[d])) : 1;
+        P->nt[d] = d < ndim ? (G.Kd[d] + P->T[d] - 1) / P->T[d] : 1;
+    }
+    P->ntiles = P->nt[0] * P->nt[1] * P->nt[2];
+}
+
+template <typename R>
+int build_lists(gbn_plan* P, const R* tm, const R* phase) {
+    typedef typename Cx<R>::T C;
+    const gbn_geometry& G = P->geom;
+    const int ndim = G.ndim;
+    const int64_t Mt = P->M_total;
+    const int ntiles = P->ntiles;
+    const int64_t nbins = (int64_t)P->F * ntiles;
+
+    std::vector<int> kf((size_t)Mt * ndim);
+    std::vector<int> gbin((size_t)Mt);
+    for (int f = 0; f < P->F; ++f) {
+        for (int64_t m = P->foff[f]; m < P->foff[f + 1]; ++m) {
+            int lin = 0, mul = 1;
+            for (int d = 0; d < ndim; ++d) {
+                const R t = tm[m * ndim + d];
+                if (!std::isfinite((double)t) || std::fabs((double)t) > 1.0e9)
+                    return fail(GBN_ERR_INVALID, "sample coordinate is not finite or out of range");
+                const int k = 1 + (int)std::floor((double)t - 0.5 * (double)G.Jd[d]);
+                kf[(size_t)m * ndim + d] = k;
+                int home = k % G.Kd[d];
+                if (home < 0) home += G.Kd[d];
+                lin += (home / P->T[d]) * mul;
+                mul *= P->nt[d];
+            }
+            gbin[(size_t)m] = f * ntiles + lin;
+        }
+    }
+    // ---- gather list: stable counting sort by home tile -------------------
+    std::vector<int64_t> gcount((size_t)nbins + 1, 0);
+    for (int64_t m = 0; m < Mt; ++m) gcount[(size_t)gbin[m] + 1]++;
+    for (int64_t b = 0; b < nbins; ++b) gcount[b + 1] += gcount[b];
+    std::vector<int64_t> gorder((size_t)Mt);
+    {
+        std::vector<int64_t> cur(gcount.begin(), gcount.end() - 1);
+        for (int64_t m = 0; m < Mt; ++m) gorder[(size_t)cur[gbin[m]]++] = m;
+    }
+    // ---- spread list: every tile a window touches ------------------------
+    // per axis: distinct tiles covered by the J window cells (wrap-aware)
+    auto axis_tiles = [&](int64_t m, int d, int* out) {
+        int n = 0;
+        for (int j = 0; j < G.Jd[d]; ++j) {
+            int c = (kf[(size_t)m * ndim + d] + j) % G.Kd[d];
+            if (c < 0) c += G.Kd[d];
+            const int tl = c / P->T[d];
+            bool seen = false;
+            for (int q = 0; q < n; ++q) seen = seen || out[q] == tl;
+            if (!seen) out[n++] = tl;
+        }
+        return n;
+    };
+    std::vector<int64_t> scount((size_t)nbins + 1, 0);
+    auto for_each_tile = [&](int64_t m, int f, auto&& fn) {
+        int tl[3][JMAX + 1];
+        int nt_[3] = {1, 1, 1};
+        for (int d = 0; d < 3; ++d) tl[d][0] = 0;
+        for (int d = 0; d < ndim; ++d) nt_[d] = axis_tiles(m, d, tl[d]);
+        for (int a2 = 0; a2 < nt_[2]; ++a2)
+            for (int a1 = 0; a1 < nt_[1]; ++a1)
+                for (int a0 = 0; a0 < nt_[0]; ++a0) {
+                    const int lin = tl[0][a0] + P->nt[0] * (tl[1][a1] + P->nt[1] * tl[2][a2]);
+                    fn(f * ntiles + lin);
+                }
+    };
+    for (int f = 0; f < P->F; ++f)
+        for (int64_t m = P->foff[f]; m < P->foff[f + 1]; ++m)
+            for_each_tile(m, f, [&](int64_t b) { scount[(size_t)b + 1]++; });
+    for (int64_t b = 0; b < nbins; ++b) scount[b + 1] += scount[b];
+    const int64_t slen = scount[(size_t)nbins];
+    std::vector<int64_t> sorder((size_t)slen);
+    {
+        std::vector<int64_t> cur(scount.begin(), scount.end() - 1);
+        for (int f = 0; f < P->F; ++f)
+            for (int64_t m = P->foff[f]; m < P->foff[f + 1]; ++m)
+                for_each_tile(m, f, [&](int64_t b) { sorder[(size_t)cur[b]++] = m; });
+    }
+    // ---- pack lists (SoA) -------------------------------------------------
+    auto pack = [&](const std::vector<int64_t>& order, DevBuf& dst, int64_t len) -> int {
+        const size_t bytes = list_bytes<R>(P, len);
+        std::vector<char> host(bytes, 0);
+        size_t off = 0;
+        if (P->has_phase) {
+            C* ph = reinterpret_cast<C*>(host.data() + off);
+            for (int64_t i = 0; i < len; ++i) {
+                ph[i].x = phase[2 * order[i]];
+                ph[i].y = phase[2 * order[i] + 1];
+            }
+            off += sizeof(C) * (size_t)len;
+        }
+        for (int d = 0; d < ndim; ++d) {
+            R* t = reinterpret_cast<R*>(host.data() + off);
+            for (int64_t i = 0; i < len; ++i) t[i] = tm[order[i] * ndim + d];
+            off += sizeof(R) * (size_t)len;
+        }
+        int* idx = reinterpret_cast<int*>(host.data() + off);
+        // sample index within its frame
+        for (int64_t i = 0; i < len; ++i) {
+            const int64_t m = order[i];
+            const int f = (int)(std::upper_bound(P->foff.begin(), P->foff.end(), m) - P->foff.begin()) - 1;
+            idx[i] = (int)(m - P->foff[f]);
+        }
+        cudaError_t e = dst.alloc(bytes);
+        if (e != cudaSuccess) return cuda_fail(e, "list allocation");
+        e = cudaMemcpy(dst.p, host.data(), bytes, cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) return cuda_fail(e, "list upload");
+        return GBN_OK;
+    };
+    int rc = pack(gorder, P->glist, Mt);
+    if (rc) return rc;
+    rc = pack(sorder, P->slist, slen);
+    if (rc) return rc;
+    P->glen = Mt;
+    P->slen = slen;
+
+    // ---- work items ---------------------------------------------------------
+    struct Item { int4 a; int2 b; };
+    std::vector<Item> gi, si;
+    std::vector<int4> rt;
+    int slots = 0;
+    for (int64_t b = 0; b < nbins; ++b) {
+        const int f = (int)(b / ntiles), tile = (int)(b % ntiles);
+        const int64_t g0 = gcount[b], gn = gcount[b + 1] - g0;
+        for (int64_t s = 0; s < gn; s += GATHER_CHUNK)
+            gi.push_back({make_int4(f, tile, (int)(g0 + s), (int)std::min<int64_t>(GATHER_CHUNK, gn - s)),
+                          make_int2(-1, 1)});
+        const int64_t s0 = scount[b], sn = scount[b + 1] - s0;
+        const int parts = (int)std::max<int64_t>(1, (sn + SPREAD_CHUNK - 1) / SPREAD_CHUNK);
+        if (parts == 1) {
+            si.push_back({make_int4(f, tile, (int)s0, (int)sn), make_int2(-1, 1)});
+        } else {
+            const int64_t per = (sn + parts - 1) / parts;
+            for (int q = 0; q < parts; ++q) {
+                const int64_t a = s0 + q * per;
+                const int64_t n = std::min<int64_t>(per, s0 + sn - a);
+                si.push_back({make_int4(f, tile, (int)a, (int)n), make_int2(slots + q, parts)});
+            }
+            rt.push_back(make_int4(f, tile, slots, parts));
+            slots += parts;
+        }
+    }
+    if (Mt > INT32_MAX || slen > INT32_MAX)
+        return fail(GBN_ERR_TOOLARGE, "more than 2^31 list entries");
+    auto heavy_first = [](const Item& x, const Item& y) { return x.a.w > y.a.w; };
+    std::stable_sort(gi.begin(), gi.end(), heavy_first);
+    std::stable_sort(si.begin(), si.end(), heavy_first);
+    std::vector<int4> ga(gi.size()), sa(si.size());
+    std::vector<int2> sb(si.size());
+    for (size_t i = 0; i < gi.size(); ++i) ga[i] = gi[i].a;
+    for (size_t i = 0; i < si.size(); ++i) {
+        sa[i] = si[i].a;
+        sb[i] = si[i].b;
+    }
+    auto upload = [&](DevBuf& dst, const void* src, size_t bytes) -> int {
+        cudaError_t e = dst.alloc(std::max<size_t>(bytes, 16));
+        if (e != cudaSuccess) return cuda_fail(e, "item allocation");
+        if (bytes) {
+            e = cudaMemcpy(dst.p, src, bytes, cudaMemcpyHostToDevice);
+            if (e != cudaSuccess) return cuda_fail(e, "item upload");
+        }
+        return GBN_OK;
+    };
+    if ((rc = upload(P->gitems, ga.data(), ga.size() * sizeof(int4)))) return rc;
+    if ((rc = upload(P->sitems, sa.data(), sa.size() * sizeof(int4)))) return rc;
+    if ((rc = upload(P->sparts, sb.data(), sb.size() * sizeof(int2)))) return rc;
+    if ((rc = upload(P->rtiles, rt.data(), rt.size() * sizeof(int4)))) return rc;
+    P->n_gitems = (int)ga.size();
+    P->n_sitems = (int)sa.size();
+    P->n_rtiles = (int)rt.size();
+    P->n_slots = slots;
+    return GBN_OK;
+}
+
+int ensure_buffers(gbn_plan* P, int coils) {
+    const int planes = P->F * coils;
+    const size_t csz = (size_t)2 * P->rsize;
+    if (planes > P->cap_planes) {
+        const size_t bytes = (size_t)planes * P->Kprod * csz;
+        cudaError_t e = P->pad.alloc(bytes);
+        if (e != cudaSuccess) return fail(GBN_ERR_NOMEM, "pad buffer allocation failed");
+        e = cudaMemset(P->pad.p, 0, bytes);
+        if (e != cudaSuccess) return cuda_fail(e, "pad buffer clear");
+        e = P->grid.alloc(bytes);
+        if (e != cudaSuccess) return fail(GBN_ERR_NOMEM, "grid buffer allocation failed");
+        P->cap_planes = planes;
+    }
+    const Lanes ln = make_lanes(P->geom.ndim, coils);
+    const int64_t tile_cells = (int64_t)P->T[0] * P->T[1] * P->T[2];
+    const int64_t chunks = (coils + ln.LS - 1) / ln.LS;
+    const int64_t need = (int64_t)P->n_slots * chunks * ln.LS * tile_cells;
+    if (need > P->scratch_cap) {
+        cudaError_t e = P->scratch.alloc((size_t)need * csz);
+        if (e != cudaSuccess) return fail(GBN_ERR_NOMEM, "scratch allocation failed");
+        P->scratch_cap = need;
+    }
+    return GBN_OK;
+}
+
+int get_fft(gbn_plan* P, int planes, cufftHandle* out) {
+    for (auto& f : P->ffts)
+        if (f.planes == planes) {
+            *out = f.h;
+            return GBN_OK;
+        }
+    const gbn_geometry& G = P->geom;
+    int n[3];
+    for (int d = 0; d < G.ndim; ++d) n[d] = G.Kd[G.ndim - 1 - d];
+    cufftHandle h;
+    cufftResult r = cufftPlanMany(&h, G.ndim, n, nullptr, 1, (int)P->Kprod, nullptr, 1, (int)P->Kprod,
+                                  P->dbl ? CUFFT_Z2Z : CUFFT_C2C, planes);
+    if (r != CUFFT_SUCCESS) return cufft_fail(r, "cufftPlanMany");
+    P->ffts.push_back({planes, h});
+    *out = h;
+    return GBN_OK;
+}
+
+int exec_fft(gbn_plan* P, cufftHandle h, void* in, void* out, int dir, cudaStream_t s) {
+    cufftResult r = cufftSetStream(h, s);
+    if (r != CUFFT_SUCCESS) return cufft_fail(r, "cufftSetStream");
+    if (P->dbl)
+        r = cufftExecZ2Z(h, (cufftDoubleComplex*)in, (cufftDoubleComplex*)out, dir);
+    else
+        r = cufftExecC2C(h, (cufftComplex*)in, (cufftComplex*)out, dir);
+    if (r != CUFFT_SUCCESS) return cufft_fail(r, "cufftExec");
+    return GBN_OK;
+}
+
+template <typename R>
+int run_gather(gbn_plan* P, const void* grid, void* y, int coils, bool phases, cudaStream_t s) {
+    typedef typename Cx<R>::T C;
+    GatherParams<R> p;
+    std::memset(&p, 0, sizeof(p));
+    p.g = make_geom<R>(P);
+    p.ln = make_lanes(P->geom.ndim, coils);
+    p.s = make_list<R>(P, P->glist, P->glen);
+    p.items = reinterpret_cast<const int4*>(P->gitems.p);
+    p.nitems = P->n_gitems;
+    p.coils = coils;
+    p.foff = reinterpret_cast<const int64_t*>(P->dfoff.p);
+    p.grid = reinterpret_cast<const C*>(grid);
+    p.y = reinterpret_cast<C*>(y);
+    p.apply_pb = phases && P->geom.phasing == GBN_PHASING_REAL;
+    p.grid_scale = (phases && P->geom.ortho) ? (R)std::sqrt((double)P->Kprod) : (R)1;
+    p.apply_ph = phases && P->has_phase;
+    GBN_CUDA(launch_gather<R>(p, s), "gather launch");
+    return GBN_OK;
+}
+
+template <typename R>
+int run_spread(gbn_plan* P, const void* y, void* grid, int coils, bool phases, cudaStream_t s) {
+    typedef typename Cx<R>::T C;
+    int rc = ensure_buffers(P, coils);
+    if (rc) return rc;
+    SpreadParams<R> p;
+    std::memset(&p, 0, sizeof(p));
+    p.g = make_geom<R>(P);
+    p.ln = make_lanes(P->geom.ndim, coils);
+    p.s = make_list<R>(P, P->slist, P->slen);
+    p.items = reinterpret_cast<const int4*>(P->sitems.p);
+    p.parts = reinterpret_cast<const int2*>(P->sparts.p);
+    p.nitems = P->n_sitems;
+    p.coils = coils;
+    p.foff = reinterpret_cast<const int64_t*>(P->dfoff.p);
+    p.y = reinterpret_cast<const C*>(y);
+    p.grid = reinterpret_cast<C*>(grid);
+    p.scratch = reinterpret_cast<C*>(P->scratch.p);
+    p.tile_cells = (int64_t)P->T[0] * P->T[1] * P->T[2];
+    p.apply_pb = phases && P->geom.phasing == GBN_PHASING_REAL;
+    p.apply_ph = phases && P->has_phase;
+    GBN_CUDA(launch_spread<R>(p, s), "spread launch");
+    if (P->n_rtiles) {
+        ReduceParams<R> q;
+        std::memset(&q, 0, sizeof(q));
+        q.g = p.g;
+        q.ln = p.ln;
+        q.tiles = reinterpret_cast<const int4*>(P->rtiles.p);
+        q.ntiles = P->n_rtiles;
+        q.coils = coils;
+        q.scratch = p.scratch;
+        q.grid = p.grid;
+        q.tile_cells = p.tile_cells;
+        q.apply_pb = p.apply_pb;
+        GBN_CUDA(launch_reduce<R>(q, s), "reduce launch");
+    }
+    return GBN_OK;
+}
+
+template <typename R>
+int run_forward(gbn_plan* P, const void* x, void* y, int coils, cudaStream_t s) {
+    int rc = ensure_buffers(P, coils);
+    if (rc) return rc;
+    const gbn_geometry& G = P->geom;
+    PadParams<R> pp;
+    std::memset(&pp, 0, sizeof(pp));
+    pp.ndim = G.ndim;
+    for (int d = 0; d < 3; ++d) {
+        pp.N[d] = d < G.ndim ? G.Nd[d] : 1;
+        pp.K[d] = d < G.ndim ? G.Kd[d] : 1;
+    }
+    pp.Nprod = P->Nprod;
+    pp.Kprod = P->Kprod;
+    pp.planes = P->F * coils;
+    pp.x = reinterpret_cast<const typename Cx<R>::T*>(x);
+    pp.sn = reinterpret_cast<const R*>(P->sn.p);
+    pp.out = reinterpret_cast<typename Cx<R>::T*>(P->pad.p);
+    GBN_CUDA(launch_pad<R>(pp, s), "pad launch");
+    cufftHandle h;
+    if ((rc = get_fft(P, P->F * coils, &h))) return rc;
+    if ((rc = exec_fft(P, h, P->pad.p, P->grid.p, CUFFT_FORWARD, s))) return rc;
+    return run_gather<R>(P, P->grid.p, y, coils, true, s);
+}
+
+template <typename R>
+int run_adjoint(gbn_plan* P, const void* y, void* x, int coils, cudaStream_t s) {
+    int rc = run_spread<R>(P, y, P->grid.p, coils, true, s);
+    if (rc) return rc;
+    cufftHandle h;
+    if ((rc = get_fft(P, P->F * coils, &h))) return rc;
+    if ((rc = exec_fft(P, h, P->grid.p, P->grid.p, CUFFT_INVERSE, s))) return rc;
+    const gbn_geometry& G = P->geom;
+    CropParams<R> cp;
+    std::memset(&cp, 0, sizeof(cp));
+    cp.ndim = G.ndim;
+    for (int d = 0; d < 3; ++d) {
+        cp.N[d] = d < G.ndim ? G.Nd[d] : 1;
+        cp.K[d] = d < G.ndim ? G.Kd[d] : 1;
+    }
+    cp.Nprod = P->Nprod;
+    cp.Kprod = P->Kprod;
+    cp.planes = P->F * coils;
+    cp.grid = reinterpret_cast<const typename Cx<R>::T*>(P->grid.p);
+    cp.sn = reinterpret_cast<const R*>(P->sn.p);
+    cp.scale = G.ortho ? (R)(G.adjoint_scale / std::sqrt((double)P->Kprod)) : (R)G.adjoint_scale;
+    cp.x = reinterpret_cast<typename Cx<R>::T*>(x);
+    GBN_CUDA(launch_crop<R>(cp, s), "crop launch");
+    return GBN_OK;
+}
+
+template <typename R>
+int upload_static(gbn_plan* P, const void* const* h_re, const void* const* h_im, const void* sn) {
+    const gbn_geometry& G = P->geom;
+    size_t total = 0;
+    for (int d = 0; d < G.ndim; ++d) total += (size_t)G.Jd[d] * G.L + 1 + 4;
+    const size_t n_tab = P->cx ? 2 * total : total;
+    std::vector<R> host(n_tab, (R)0);
+    size_t off = 0;
+    for (int part = 0; part < (P->cx ? 2 : 1); ++part) {
+        for (int d = 0; d < G.ndim; ++d) {
+            const size_t len = (size_t)G.Jd[d] * G.L + 1;
+            const R* src = reinterpret_cast<const R*>(part == 0 ? h_re[d] : h_im[d]);
+            if (!src) return fail(GBN_ERR_INVALID, "missing lookup table");
+            std::memcpy(host.data() + off + 2, src, len * sizeof(R));
+            off += len + 4;
+        }
+    }
+    cudaError_t e = P->tables.alloc(n_tab * sizeof(R));
+    if (e != cudaSuccess) return cuda_fail(e, "table allocation");
+    GBN_CUDA(cudaMemcpy(P->tables.p, host.data(), n_tab * sizeof(R), cudaMemcpyHostToDevice), "table upload");
+    e = P->sn.alloc((size_t)P->Nprod * sizeof(R));
+    if (e != cudaSuccess) return cuda_fail(e, "sn allocation");
+    if (!sn) return fail(GBN_ERR_INVALID, "missing deapodisation array");
+    GBN_CUDA(cudaMemcpy(P->sn.p, sn, (size_t)P->Nprod * sizeof(R), cudaMemcpyHostToDevice), "sn upload");
+    e = P->dfoff.alloc(P->foff.size() * sizeof(int64_t));
+    if (e != cudaSuccess) return cuda_fail(e, "offset allocation");
+    GBN_CUDA(cudaMemcpy(P->dfoff.p, P->foff.data(), P->foff.size() * sizeof(int64_t), cudaMemcpyHostToDevice),
+             "offset upload");
+    return GBN_OK;
+}
+
+int validate(const gbn_geometry* g) {
+    if (!g) return fail(GBN_ERR_INVALID, "null geometry");
+    if (g->ndim < 1 || g->ndim > 3) return fail(GBN_ERR_UNSUPPORTED, "ndim must be 1, 2 or 3");
+    if (g->precision != GBN_PRECISION_SINGLE && g->precision != GBN_PRECISION_DOUBLE)
+        return fail(GBN_ERR_INVALID, "precision must be single or double");
+    if (g->phasing != GBN_PHASING_REAL && g->phasing != GBN_PHASING_COMPLEX)
+        return fail(GBN_ERR_INVALID, "phasing must be real or complex");
+    if (g->L < 1) return fail(GBN_ERR_INVALID, "table oversampling L must be >= 1");
+    if (g->n_frames < 1) return fail(GBN_ERR_INVALID, "n_frames must be >= 1");
+    if (g->max_coils < 1) return fail(GBN_ERR_INVALID, "max_coils must be >= 1");
+    int64_t K = 1;
+    for (int d = 0; d < g->ndim; ++d) {
+        if (g->Nd[d] < 1 || g->Kd[d] < 1) return fail(GBN_ERR_INVALID, "sizes must be positive");
+        if (g->Kd[d] < g->Nd[d]) return fail(GBN_ERR_INVALID, "Kd must be >= Nd on every axis");
+        if (g->Jd[d] < 1) return fail(GBN_ERR_INVALID, "kernel width J must be >= 1");
+        if (g->Jd[d] > JMAX) return fail(GBN_ERR_UNSUPPORTED, "kernel width J > 8 is not built");
+        if (g->Jd[d] > g->Kd[d]) return fail(GBN_ERR_INVALID, "kernel width J exceeds Kd");
+        if (g->tile[d] < 0) return fail(GBN_ERR_INVALID, "tile edges must be >= 0");
+        K *= g->Kd[d];
+        if (g->pb_order[d] < 0 || g->pb_order[d] >= g->ndim)
+            return fail(GBN_ERR_INVALID, "pb_order entries must name axes");
+    }
+    if (K > INT32_MAX) return fail(GBN_ERR_TOOLARGE, "prod(Kd) must be < 2^31");
+    if ((int64_t)g->L * JMAX > (1 << 28)) return fail(GBN_ERR_TOOLARGE, "table too long");
+    return GBN_OK;
+}
+
+template <typename R>
+int plan_points(gbn_plan* P, const void* tm, const void* phase) {
+    if (!tm && P->M_total > 0) return fail(GBN_ERR_INVALID, "null coordinate array");
+    P->has_phase = phase != nullptr;
+    return build_lists<R>(P, reinterpret_cast<const R*>(tm), reinterpret_cast<const R*>(phase));
+}
+
+}  // namespace
+
+namespace {
+template <typename R>
+int run_grad(gbn_plan* P, const void* grid, const void* gy, const double* shift, void* gtm, int coils,
+             cudaStream_t s) {
+    typedef typename Cx<R>::T C;
+    GradParams<R> p;
+    std::memset(&p, 0, sizeof(p));
+    p.g = make_geom<R>(P);
+    const SampleList<R> L = make_list<R>(P, P->glist, P->glen);
+    const R* db = reinterpret_cast<const R*>(P->dtables.p);
+    size_t off = 0;
+    for (int d = 0; d < P->geom.ndim; ++d) {
+        p.t[d] = L.t[d];
+        p.dh[d] = db + off + 2;
+        off += (size_t)P->geom.Jd[d] * P->geom.L + 1 + 4;
+        p.phase_shift[d] = shift ? (R)shift[d] : (R)0;
+    }
+    p.idx = L.idx;
+    p.ph = L.ph;
+    p.M = P->glen;
+    p.coils = coils;
+    p.apply_pb = P->geom.phasing == GBN_PHASING_REAL;
+    p.grid_scale = P->geom.ortho ? (R)std::sqrt((double)P->Kprod) : (R)1;
+    p.grid = reinterpret_cast<const C*>(grid);
+    p.gy = reinterpret_cast<const C*>(gy);
+    p.gtm = reinterpret_cast<R*>(gtm);
+    GBN_CUDA(launch_grad<R>(p, s), "gradient launch");
+    return GBN_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int gbn_plan_create(gbn_plan** out, const gbn_geometry* geom, const void* const* h_re,
+                    const void* const* h_im, const void* sn, const int64_t* frame_offsets,
+                    const void* tm, const void* sample_phase, int device) {
+    if (!out) return fail(GBN_ERR_INVALID, "null plan pointer");
+    *out = nullptr;
+    int rc = validate(geom);
+    if (rc) return rc;
+    if (!h_re || !frame_offsets) return fail(GBN_ERR_INVALID, "null table or offset array");
+    DeviceGuard guard(device);
+    gbn_plan* P = new (std::nothrow) gbn_plan();
+    if (!P) return fail(GBN_ERR_NOMEM, "host allocation failed");
+    P->device = device;
+    P->geom = *geom;
+    P->dbl = geom->precision == GBN_PRECISION_DOUBLE;
+    P->rsize = P->dbl ? 8 : 4;
+    P->cx = geom->phasing == GBN_PHASING_COMPLEX;
+    if (P->cx && (!h_im || !h_im[0])) {
+        delete P;
+        return fail(GBN_ERR_INVALID, "complex phasing needs imaginary tables");
+    }
+    P->F = geom->n_frames;
+    P->foff.assign(frame_offsets, frame_offsets + P->F + 1);
+    if (P->foff[0] != 0) {
+        delete P;
+        return fail(GBN_ERR_INVALID, "frame_offsets[0] must be 0");
+    }
+    for (int f = 0; f < P->F; ++f)
+        if (P->foff[f + 1] < P->foff[f]) {
+            delete P;
+            return fail(GBN_ERR_INVALID, "frame offsets must be non-decreasing");
+        }
+    P->M_total = P->foff[P->F];
+    for (int d = 0; d < geom->ndim; ++d) {
+        P->Kprod *= geom->Kd[d];
+        P->Nprod *= geom->Nd[d];
+    }
+    choose_tiles(P);
+    rc = P->dbl ? upload_static<double>(P, h_re, h_im, sn) : upload_static<float>(P, h_re, h_im, sn);
+    if (!rc) rc = P->dbl ? plan_points<double>(P, tm, sample_phase) : plan_points<float>(P, tm, sample_phase);
+    if (rc) {
+        delete P;
+        return rc;
+    }
+    *out = P;
+    return GBN_OK;
+}
+
+int gbn_plan_set_points(gbn_plan* P, const void* tm, const void* sample_phase) {
+    if (!P) return fail(GBN_ERR_INVALID, "null plan");
+    std::lock_guard<std::mutex> lk(P->mu);
+    DeviceGuard guard(P->device);
+    GBN_CUDA(cudaDeviceSynchronize(), "synchronise before replanning");
+    return P->dbl ? plan_points<double>(P, tm, sample_phase) : plan_points<float>(P, tm, sample_phase);
+}
+
+int gbn_plan_destroy(gbn_plan* P) {
+    if (!P) return GBN_OK;
+    DeviceGuard guard(P->device);
+    cudaDeviceSynchronize();
+    delete P;
+    return GBN_OK;
+}
+
+static int check_call(gbn_plan* P, const void* a, const void* b, int coils) {
+    if (!P) return fail(GBN_ERR_INVALID, "null plan");
+    if (coils < 1) return fail(GBN_ERR_INVALID, "coils must be >= 1");
+    if ((!a || !b) && P->M_total > 0) return fail(GBN_ERR_INVALID, "null data pointer");
+    if ((int64_t)coils * P->F * P->Kprod > ((int64_t)1 << 40))
+        return fail(GBN_ERR_TOOLARGE, "batch too large");
+    return GBN_OK;
+}
+
+int gbn_forward(gbn_plan* P, const void* x, void* y, int coils, void* stream) {
+    int rc = check_call(P, x, y, coils);
+    if (rc) return rc;
+    std::lock_guard<std::mutex> lk(P->mu);
+    DeviceGuard guard(P->device);
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    return P->dbl ? run_forward<double>(P, x, y, coils, s) : run_forward<float>(P, x, y, coils, s);
+}
+
+int gbn_adjoint(gbn_plan* P, const void* y, void* x, int coils, void* stream) {
+    int rc = check_call(P, y, x, coils);
+    if (rc) return rc;
+    std::lock_guard<std::mutex> lk(P->mu);
+    DeviceGuard guard(P->device);
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    return P->dbl ? run_adjoint<double>(P, y, x, coils, s) : run_adjoint<float>(P, y, x, coils, s);
+}
+
+int gbn_interp_forward(gbn_plan* P, const void* grid, void* y, int coils, void* stream) {
+    int rc = check_call(P, grid, y, coils);
+    if (rc) return rc;
+    std::lock_guard<std::mutex> lk(P->mu);
+    DeviceGuard guard(P->device);
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    return P->dbl ? run_gather<double>(P, grid, y, coils, false, s)
+                  : run_gather<float>(P, grid, y, coils, false, s);
+}
+
+int gbn_interp_adjoint(gbn_plan* P, const void* y, void* grid, int coils, void* stream) {
+    int rc = check_call(P, y, grid, coils);
+    if (rc) return rc;
+    std::lock_guard<std::mutex> lk(P->mu);
+    DeviceGuard guard(P->device);
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    return P->dbl ? run_spread<double>(P, y, grid, coils, false, s)
+                  : run_spread<float>(P, y, grid, coils, false, s);
+}
+
+int gbn_forward_grid(gbn_plan* P, void** grid) {
+    if (!P || !grid) return fail(GBN_ERR_INVALID, "null argument");
+    *grid = P->grid.p;
+    return GBN_OK;
+}
+
+int gbn_plan_set_dtables(gbn_plan* P, const void* const* dtab) {
+    if (!P || !dtab) return fail(GBN_ERR_INVALID, "null argument");
+    std::lock_guard<std::mutex> lk(P->mu);
+    DeviceGuard guard(P->device);
+    const gbn_geometry& G = P->geom;
+    size_t total = 0;
+    for (int d = 0; d < G.ndim; ++d) total += (size_t)G.Jd[d] * G.L + 1 + 4;
+    std::vector<char> host(total * P->rsize, 0);
+    size_t off = 0;
+    for (int d = 0; d < G.ndim; ++d) {
+        const size_t len = (size_t)G.Jd[d] * G.L + 1;
+        if (!dtab[d]) return fail(GBN_ERR_INVALID, "missing derivative table");
+        std::memcpy(host.data() + (off + 2) * P->rsize, dtab[d], len * P->rsize);
+        off += len + 4;
+    }
+    cudaError_t e = P->dtables.alloc(host.size());
+    if (e != cudaSuccess) return cuda_fail(e, "derivative table allocation");
+    GBN_CUDA(cudaMemcpy(P->dtables.p, host.data(), host.size(), cudaMemcpyHostToDevice),
+             "derivative table upload");
+    return GBN_OK;
+}
+
+
+int gbn_grad_tm(gbn_plan* P, const void* grid, const void* gy, const double* phase_shift, void* gtm,
+                int coils, void* stream) {
+    int rc = check_call(P, grid, gy, coils);
+    if (rc) return rc;
+    if (!gtm && P->M_total > 0) return fail(GBN_ERR_INVALID, "null gradient output");
+    if (P->F != 1) return fail(GBN_ERR_UNSUPPORTED, "coordinate gradient needs a single-frame plan");
+    if (P->cx) return fail(GBN_ERR_UNSUPPORTED, "coordinate gradient needs phasing real");
+    if (!P->dtables.p) return fail(GBN_ERR_INVALID, "derivative tables not set (gbn_plan_set_dtables)");
+    std::lock_guard<std::mutex> lk(P->mu);
+    DeviceGuard guard(P->device);
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    return P->dbl ? run_grad<double>(P, grid, gy, phase_shift, gtm, coils, s)
+                  : run_grad<float>(P, grid, gy, phase_shift, gtm, coils, s);
+}
+
+int gbn_dtft_forward(int ndim, const int* Nd, const double* n_shift, const void* omega, int64_t M,
+                     const void* x, void* y, int reps, void* stream) {
+    if (ndim < 1 || ndim > 3 || !Nd || !n_shift || M < 0 || reps < 1)
+        return fail(GBN_ERR_INVALID, "bad dtft arguments");
+    if (M > 0 && (!omega || !x || !y)) return fail(GBN_ERR_INVALID, "null dtft pointer");
+    GBN_CUDA(launch_dtft(false, ndim, Nd, n_shift, (const double*)omega, M, (const double2*)x, (double2*)y, reps,
+                         reinterpret_cast<cudaStream_t>(stream)),
+             "dtft forward");
+    return GBN_OK;
+}
+
+int gbn_dtft_adjoint(int ndim, const int* Nd, const double* n_shift, const void* omega, int64_t M,
+                     const void* y, void* x, int reps, void* stream) {
+    if (ndim < 1 || ndim > 3 || !Nd || !n_shift || M < 0 || reps < 1)
+        return fail(GBN_ERR_INVALID, "bad dtft arguments");
+    if (!x || (M > 0 && (!omega || !y))) return fail(GBN_ERR_INVALID, "null dtft pointer");
+    GBN_CUDA(launch_dtft(true, ndim, Nd, n_shift, (const double*)omega, M, (const double2*)y, (double2*)x, reps,
+                         reinterpret_cast<cudaStream_t>(stream)),
+             "dtft adjoint");
+    return GBN_OK;
+}
+
+int gbn_plan_stats(const gbn_plan* P, int64_t* o) {
+    if (!P || !o) return fail(GBN_ERR_INVALID, "null argument");
+    o[0] = P->n_gitems;
+    o[1] = P->n_sitems;
+    o[2] = P->n_rtiles;
+    o[3] = P->glen;
+    o[4] = P->slen;
+    o[5] = (int64_t)P->ntiles * P->F;
+    o[6] = (int64_t)(P->tables.bytes + P->sn.bytes + P->glist.bytes + P->slist.bytes + P->pad.bytes +
+                     P->grid.bytes + P->scratch.bytes);
+    o[7] = P->M_total;
+    return GBN_OK;
+}
+
+const char* gbn_last_error(void) { return g_last_error.c_str(); }
+
+const char* gbn_version(void) { return "gbnufft 0.1.0 (sm_103a)"; }
+
+}  // extern "C"
