@@ -55,8 +55,8 @@ class NufftBase(object):
     docstring for the data conventions.  ``mode`` must be ``'table'``.
 
     Extra keyword (not in the reference): ``max_coils`` -- the repetition
-    count the tile plan is sized for (default 1; larger batches re-tile once
-    automatically).
+    count the tile plan is sized for (default 1).  Any batch size works; a
+    batch wider than the tiles were sized for runs in more coil chunks.
     """
 
     def __init__(self, Nd, omega, Jd=4, Kd=None, precision="single", mode="table", Ld=1024,
@@ -253,9 +253,18 @@ class NufftBase(object):
                 arr = arr.astype(self._cplx_dtype)
             t = None
         total = (t.numel() if t is not None else arr.size)
-        if total % narg != 0:
+        if narg == 0:
+            # empty sample set: repetitions come from the trailing axis, if any
+            shp = tuple(t.shape) if t is not None else arr.shape
+            if total != 0:
+                raise ValueError("Input signal has the wrong size.")
+            reps = int(shp[-1]) if len(shp) == 2 else 1
+        elif total % narg != 0:
             raise ValueError("Input signal has the wrong size.")
-        reps = total // narg
+        else:
+            reps = total // narg
+        if reps < 1:
+            raise ValueError("Input signal has the wrong size.")
         full = tuple(leading_shape) + (reps,)
         if t is not None:
             t = t.reshape(full) if t.dim() != len(full) or tuple(t.shape) != full else t

@@ -75,7 +75,9 @@ template <typename R, bool CX>
 __device__ __forceinline__ void table_coef(const Geom<R>& g, int d, R t, int k, R& cr, R& ci) {
     const R pp = (t - (R)k) * (R)g.L;
     const R nf = floor(pp);
-    const int n = (int)nf + g.ncenter[d];
+    // the host bounds |t| so this index lies in [-1, J*L+1]; the clamp keeps
+    // every read inside the zero-padded table regardless
+    const int n = min(max((int)nf + g.ncenter[d], -2), g.J[d] * g.L + 1);
     const R alf = pp - nf;
     const R* h = g.hr[d];
     cr = ((R)1 - alf) * __ldg(h + n) + alf * __ldg(h + n + 1);

@@ -45,7 +45,7 @@ __global__ void __launch_bounds__(128) grad_kernel(const GradParams<R> p) {
                 table_coef<R, false>(g, d, t[d], kf[d] + j, c[d][j], ci);
                 const R pp = (t[d] - (R)(kf[d] + j)) * (R)g.L;
                 const R nf = floor(pp);
-                const int n = (int)nf + g.ncenter[d];
+                const int n = min(max((int)nf + g.ncenter[d], -2), g.J[d] * g.L + 1);
                 const R alf = pp - nf;
                 dc[d][j] = ((R)1 - alf) * __ldg(p.dh[d] + n) + alf * __ldg(p.dh[d] + n + 1);
             }

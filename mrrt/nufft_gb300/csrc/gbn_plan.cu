@@ -93,7 +93,11 @@ struct FftEntry {
 
 constexpr int GATHER_CHUNK = 512;   // samples per gather work item
 constexpr int SPREAD_CHUNK = 512;   // list entries per spread work item
-constexpr size_t SMEM_BUDGET = 112 * 1024;
+constexpr size_t SMEM_BUDGET = 112 * 1024;   // tile choice: two CTAs per SM
+constexpr size_t SMEM_LIMIT = 227 * 1024;    // per-CTA hardware limit
+// |tm| bound: keeps t - k exact in float32 (both below 2^24) so table indices
+// stay inside the table.
+constexpr double TM_LIMIT = 4194304.0;
 
 }  // namespace
 
@@ -258,8 +262,8 @@ int build_lists(gbn_plan* P, const R* tm, const R* phase) {
             int lin = 0, mul = 1;
             for (int d = 0; d < ndim; ++d) {
                 const R t = tm[m * ndim + d];
-                if (!std::isfinite((double)t) || std::fabs((double)t) > 1.0e9)
-                    return fail(GBN_ERR_INVALID, "sample coordinate is not finite or out of range");
+                if (!std::isfinite((double)t) || std::fabs((double)t) > TM_LIMIT)
+                    return fail(GBN_ERR_INVALID, "sample coordinate is not finite or |tm| > 2^22");
                 const int k = 1 + (int)std::floor((double)t - 0.5 * (double)G.Jd[d]);
                 kf[(size_t)m * ndim + d] = k;
                 int home = k % G.Kd[d];
@@ -414,6 +418,24 @@ int build_lists(gbn_plan* P, const R* tm, const R* phase) {
     return GBN_OK;
 }
 
+// Scratch for the partial tiles of split spread work items.
+int ensure_scratch(gbn_plan* P, int coils) {
+    const size_t csz = (size_t)2 * P->rsize;
+    const Lanes ln = make_lanes(P->geom.ndim, coils);
+    const int64_t tile_cells = (int64_t)P->T[0] * P->T[1] * P->T[2];
+    const int64_t chunks = (coils + ln.LS - 1) / ln.LS;
+    // an upper bound for any lane count call_lanes may pick (halving LS
+    // never increases chunks * LS)
+    const int64_t need = (int64_t)P->n_slots * chunks * ln.LS * tile_cells;
+    if (need > P->scratch_cap) {
+        cudaError_t e = P->scratch.alloc((size_t)need * csz);
+        if (e != cudaSuccess) return fail(GBN_ERR_NOMEM, "scratch allocation failed");
+        P->scratch_cap = need;
+    }
+    return GBN_OK;
+}
+
+// Zero-padded FFT input, FFT output grid and scratch for F * coils planes.
 int ensure_buffers(gbn_plan* P, int coils) {
     const int planes = P->F * coils;
     const size_t csz = (size_t)2 * P->rsize;
@@ -427,16 +449,7 @@ int ensure_buffers(gbn_plan* P, int coils) {
         if (e != cudaSuccess) return fail(GBN_ERR_NOMEM, "grid buffer allocation failed");
         P->cap_planes = planes;
     }
-    const Lanes ln = make_lanes(P->geom.ndim, coils);
-    const int64_t tile_cells = (int64_t)P->T[0] * P->T[1] * P->T[2];
-    const int64_t chunks = (coils + ln.LS - 1) / ln.LS;
-    const int64_t need = (int64_t)P->n_slots * chunks * ln.LS * tile_cells;
-    if (need > P->scratch_cap) {
-        cudaError_t e = P->scratch.alloc((size_t)need * csz);
-        if (e != cudaSuccess) return fail(GBN_ERR_NOMEM, "scratch allocation failed");
-        P->scratch_cap = need;
-    }
-    return GBN_OK;
+    return ensure_scratch(P, coils);
 }
 
 int get_fft(gbn_plan* P, int planes, cufftHandle* out) {
@@ -468,13 +481,24 @@ int exec_fft(gbn_plan* P, cufftHandle h, void* in, void* out, int dir, cudaStrea
     return GBN_OK;
 }
 
+// Coil lanes for a call: as many as the coil count asks for, halved until
+// the gather and spread shared memory fit the per-CTA limit with the plan's
+// tiles (a plan tiled for few coils still runs wide batches, in more chunks).
+template <typename R>
+Lanes call_lanes(const gbn_plan* P, const Geom<R>& g, int coils) {
+    Lanes ln = make_lanes(P->geom.ndim, coils);
+    while (ln.LS > 1 && (gather_smem<R>(g, ln) > SMEM_LIMIT || spread_smem<R>(g, ln) > SMEM_LIMIT))
+        ln = make_lanes(P->geom.ndim, ln.LS / 2);
+    return ln;
+}
+
 template <typename R>
 int run_gather(gbn_plan* P, const void* grid, void* y, int coils, bool phases, cudaStream_t s) {
     typedef typename Cx<R>::T C;
     GatherParams<R> p;
     std::memset(&p, 0, sizeof(p));
     p.g = make_geom<R>(P);
-    p.ln = make_lanes(P->geom.ndim, coils);
+    p.ln = call_lanes<R>(P, p.g, coils);
     p.s = make_list<R>(P, P->glist, P->glen);
     p.items = reinterpret_cast<const int4*>(P->gitems.p);
     p.nitems = P->n_gitems;
@@ -492,12 +516,12 @@ int run_gather(gbn_plan* P, const void* grid, void* y, int coils, bool phases, c
 template <typename R>
 int run_spread(gbn_plan* P, const void* y, void* grid, int coils, bool phases, cudaStream_t s) {
     typedef typename Cx<R>::T C;
-    int rc = ensure_buffers(P, coils);
+    int rc = ensure_scratch(P, coils);
     if (rc) return rc;
     SpreadParams<R> p;
     std::memset(&p, 0, sizeof(p));
     p.g = make_geom<R>(P);
-    p.ln = make_lanes(P->geom.ndim, coils);
+    p.ln = call_lanes<R>(P, p.g, coils);
     p.s = make_list<R>(P, P->slist, P->slen);
     p.items = reinterpret_cast<const int4*>(P->sitems.p);
     p.parts = reinterpret_cast<const int2*>(P->sparts.p);
@@ -532,6 +556,7 @@ template <typename R>
 int run_forward(gbn_plan* P, const void* x, void* y, int coils, cudaStream_t s) {
     int rc = ensure_buffers(P, coils);
     if (rc) return rc;
+    if (!P->pad.p || !P->grid.p) return fail(GBN_ERR_NOMEM, "transform buffers missing");
     const gbn_geometry& G = P->geom;
     PadParams<R> pp;
     std::memset(&pp, 0, sizeof(pp));
@@ -555,7 +580,12 @@ int run_forward(gbn_plan* P, const void* x, void* y, int coils, cudaStream_t s) 
 
 template <typename R>
 int run_adjoint(gbn_plan* P, const void* y, void* x, int coils, cudaStream_t s) {
-    int rc = run_spread<R>(P, y, P->grid.p, coils, true, s);
+    // allocate first: the grid pointer handed to the spread must be the
+    // buffer this call will use (it is null before the first call)
+    int rc = ensure_buffers(P, coils);
+    if (rc) return rc;
+    if (!P->grid.p) return fail(GBN_ERR_NOMEM, "grid buffer missing");
+    rc = run_spread<R>(P, y, P->grid.p, coils, true, s);
     if (rc) return rc;
     cufftHandle h;
     if ((rc = get_fft(P, P->F * coils, &h))) return rc;
