@@ -62,7 +62,8 @@ typedef struct gbn_geometry {
     double pb_coef[3];
     int pb_order[3];
     int n_frames;          /* number of sample sets (1 for a plain operator) */
-    int tile[3];           /* tile edge per memory axis, 0 = default          */
+    int tile[3];           /* gather tile edge per memory axis, 0 = default   */
+    int stile[3];          /* spread tile edge per memory axis, 0 = default   */
     int max_coils;         /* largest coil count a call will use              */
     int flags;             /* reserved, 0                                     */
 } gbn_geometry;

@@ -37,6 +37,7 @@ class GbnGeometry(ctypes.Structure):
         ("pb_order", ctypes.c_int * 3),
         ("n_frames", ctypes.c_int),
         ("tile", ctypes.c_int * 3),
+        ("stile", ctypes.c_int * 3),
         ("max_coils", ctypes.c_int),
         ("flags", ctypes.c_int),
     ]

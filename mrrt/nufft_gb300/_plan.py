@@ -38,7 +38,7 @@ class GpuPlan:
 
     def __init__(self, Nd, Kd, Jd, L, rdt, tables_re, tables_im, sn, tm, sample_phase,
                  frame_offsets=None, ortho=False, adjoint_scale=1.0, pb_coef=None, pb_order=None,
-                 phasing="real", max_coils=1, tile=None, device=None):
+                 phasing="real", max_coils=1, tile=None, stile=None, device=None):
         require_cuda()
         self.lib = _lib.load()
         self.rdt = np.dtype(rdt)
@@ -50,6 +50,7 @@ class GpuPlan:
         for d in range(self.ndim):
             g.Nd[d], g.Kd[d], g.Jd[d] = int(Nd[d]), int(Kd[d]), int(Jd[d])
             g.tile[d] = int(tile[d]) if tile is not None else 0
+            g.stile[d] = int(stile[d]) if stile is not None else 0
             g.pb_coef[d] = float(pb_coef[d]) if pb_coef is not None else 0.0
             g.pb_order[d] = int(pb_order[d]) if pb_order is not None else d
         g.L = int(L)

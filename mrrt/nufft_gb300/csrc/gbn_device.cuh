@@ -113,14 +113,7 @@ __device__ __forceinline__ int region_dims(const Geom<R>& g, int ndim, int* Rd) 
 
 // Complex FMA helpers: acc += c * v with c = (cr, ci) (ci == 0 when !CX).
 template <bool CX, typename C, typename R>
-__device__ __forceinline__ void cfma(C& acc, R cr, R ci, C v) {
-    acc.x += cr * v.x;
-    acc.y += cr * v.y;
-    if (CX) {
-        acc.x -= ci * v.y;
-        acc.y += ci * v.x;
-    }
-}
+__device__ __forceinline__ void cfma(C& acc, R cr, R ci, C v);
 // acc += conj(c) * v
 template <bool CX, typename C, typename R>
 __device__ __forceinline__ C cscale_conj(R cr, R ci, C v) {
@@ -132,6 +125,49 @@ __device__ __forceinline__ C cscale_conj(R cr, R ci, C v) {
         r.y -= ci * v.x;
     }
     return r;
+}
+
+
+// Packed single-precision pairs (Blackwell f32x2 pipe): one instruction for
+// two IEEE round-to-nearest operations, bitwise identical to two scalar
+// fmaf / multiplications.
+__device__ __forceinline__ float2 ffma2(float2 a, float2 b, float2 c) {
+    unsigned long long ra, rb, rc, rd;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(ra) : "f"(a.x), "f"(a.y));
+    asm("mov.b64 %0, {%1, %2};" : "=l"(rb) : "f"(b.x), "f"(b.y));
+    asm("mov.b64 %0, {%1, %2};" : "=l"(rc) : "f"(c.x), "f"(c.y));
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(rd) : "l"(ra), "l"(rb), "l"(rc));
+    float2 d;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(d.x), "=f"(d.y) : "l"(rd));
+    return d;
+}
+__device__ __forceinline__ float2 fmul2(float2 a, float2 b) {
+    unsigned long long ra, rb, rd;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(ra) : "f"(a.x), "f"(a.y));
+    asm("mov.b64 %0, {%1, %2};" : "=l"(rb) : "f"(b.x), "f"(b.y));
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(rd) : "l"(ra), "l"(rb));
+    float2 d;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(d.x), "=f"(d.y) : "l"(rd));
+    return d;
+}
+// c * v + acc for real c and complex v, acc (pair ops in single precision)
+__device__ __forceinline__ float2 rcfma(float c, float2 v, float2 acc) { return ffma2(make_float2(c, c), v, acc); }
+__device__ __forceinline__ double2 rcfma(double c, double2 v, double2 acc) {
+    return make_double2(fma(c, v.x, acc.x), fma(c, v.y, acc.y));
+}
+__device__ __forceinline__ float2 rcmul(float c, float2 v) { return fmul2(make_float2(c, c), v); }
+__device__ __forceinline__ double2 rcmul(double c, double2 v) { return make_double2(c * v.x, c * v.y); }
+
+template <bool CX, typename C, typename R>
+__device__ __forceinline__ void cfma(C& acc, R cr, R ci, C v) {
+    if (CX) {
+        acc.x += cr * v.x;
+        acc.y += cr * v.y;
+        acc.x -= ci * v.y;
+        acc.y += ci * v.x;
+    } else {
+        acc = rcfma(cr, v, acc);
+    }
 }
 
 }  // namespace gbn

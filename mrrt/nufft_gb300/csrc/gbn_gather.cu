@@ -9,9 +9,15 @@
 //   LS coils; the lanes of a warp are (sample slot, coil), so a sample's
 //   J^d coefficients are computed once and applied to LS coils;
 // * the tile plus its (J-1)-cell halo is staged once in shared memory for
-//   all LS coils, with phase_before and the orthonormal scale applied while
-//   staging; every sample of the tile then reads its window from shared
-//   memory.
+//   all LS coils ([cell][coil], padded row), with phase_before and the
+//   orthonormal scale applied while staging;
+// * a warp prepares 32 samples at a time, one per lane (coefficients,
+//   window position, output index, phase), then gathers them SW at a time
+//   from shared memory, reading the prepared values by shuffle.
+//
+// The kernel is compiled generically (run-time kernel width J <= 8 and lane
+// count) and, for the common single-precision real-kernel cases, with J and
+// the lane count fixed at compile time (no predication, constant strides).
 #include <cuda_runtime.h>
 
 #include "gbn_device.cuh"
@@ -21,20 +27,21 @@ namespace gbn {
 
 constexpr int GATHER_THREADS = 256;
 
-// ---------------------------------------------------------------------------
-// forward gather
-// ---------------------------------------------------------------------------
-template <typename R, int NDIM, bool CX>
+template <typename R, int NDIM, bool CX, int JJ, int LSC>
 __global__ void __launch_bounds__(GATHER_THREADS)
 gather_kernel(const GatherParams<R> p) {
     typedef typename Cx<R>::T C;
+    constexpr int JL = JJ > 0 ? JJ : JMAX;    // loop bound of the tap loops
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C* S = reinterpret_cast<C*>(smem_raw);
     const Geom<R>& g = p.g;
 
     const int4 it = p.items[blockIdx.x];
     const int f = it.x, tile = it.y, start = it.z, count = it.w;
-    const int LS = p.ln.LS, lsh = p.ln.lsh, LSP = p.ln.LSP, swz = p.ln.swz;
+    const int LS = LSC > 0 ? LSC : p.ln.LS;
+    const int lsh = LSC > 0 ? (LSC == 32 ? 5 : LSC == 16 ? 4 : LSC == 8 ? 3 : LSC == 4 ? 2 : LSC == 2 ? 1 : 0)
+                            : p.ln.lsh;
+    const int LSP = LSC > 0 ? (LSC == 1 ? 1 : LSC + 1) : p.ln.LSP;
     const int c0 = blockIdx.y << lsh;
     const int nc = min(LS, p.coils - c0);
 
@@ -43,7 +50,8 @@ gather_kernel(const GatherParams<R> p) {
     int Rd[3];
     const int Rtot = region_dims(g, NDIM, Rd);
 
-    // ---- stage tile + halo for nc coils -----------------------------------
+    // ---- stage tile + halo for nc coils: thread per cell, coils in batches
+    // of four independent loads ----------------------------------------------
     const C* gb = p.grid + ((int64_t)f * p.coils + c0) * g.Kprod;
     for (int cell = threadIdx.x; cell < Rtot; cell += blockDim.x) {
         int r[3];
@@ -62,21 +70,30 @@ gather_kernel(const GatherParams<R> p) {
         }
         C ph = cmake<R>((R)1, (R)0);
         if (p.apply_pb) ph = phase_before(g, k);
-        C* dst = S + (int64_t)cell * LSP;
-        const int sw = cell & swz;
-        for (int c = 0; c < nc; ++c) {
-            C v = gb[(int64_t)c * g.Kprod + off];
-            if (p.apply_pb) v = cmul(v, ph);
-            if (p.grid_scale != (R)1) {
-                v.x = v.x / p.grid_scale;
-                v.y = v.y / p.grid_scale;
+        const int dst = cell * LSP;
+        const C* src = gb + off;
+        for (int c = 0; c < nc; c += 4) {
+            C v[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                if (c + u < nc) v[u] = src[(int64_t)(c + u) * g.Kprod];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                if (c + u < nc) {
+                    C w = v[u];
+                    if (p.apply_pb) w = cmul(w, ph);
+                    if (p.grid_scale != (R)1) {
+                        w.x = w.x / p.grid_scale;
+                        w.y = w.y / p.grid_scale;
+                    }
+                    S[dst + c + u] = w;
+                }
             }
-            dst[c ^ sw] = v;
         }
     }
     __syncthreads();
 
-    // ---- per-sample gather from shared memory -----------------------------
+    // ---- per-sample gather from shared memory -------------------------------
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int nwarps = blockDim.x >> 5;
     const int SW = 32 >> lsh;
@@ -84,86 +101,101 @@ gather_kernel(const GatherParams<R> p) {
     const int64_t fo = p.foff[f];
     const int Mf = (int)(p.foff[f + 1] - fo);
     C* yb = p.y + fo * p.coils + (int64_t)(c0 + coil) * Mf;
+    const int J0 = JJ > 0 ? JJ : g.J[0];
+    const int J1 = JJ > 0 ? JJ : g.J[NDIM > 1 ? 1 : 0];
+    const int J2 = JJ > 0 ? JJ : g.J[NDIM > 2 ? 2 : 0];
+    const int rowstride = Rd[0] * LSP;
+    const int planestride = Rd[0] * Rd[1] * LSP;
 
-    for (int i0 = warp * SW; i0 < count; i0 += nwarps * SW) {
-        const int i = i0 + slot;
-        if (i >= count) continue;
-        const int e = start + i;
-        R t[3];
-        int kf[3], loc[3];
+    for (int base = warp * 32; base < count; base += nwarps * 32) {
+        const int nb = min(32, count - base);
+        R mcr[NDIM][JL], mci[NDIM][JL];
+        int mbase = 0;  // shared-memory index of the window's first cell
+        int midx = 0;
+        C mph = cmake<R>((R)1, (R)0);
 #pragma unroll
-        for (int d = 0; d < NDIM; ++d) {
-            t[d] = p.s.t[d][e];
-            kf[d] = first_tap(t[d], g.J[d]);
-            loc[d] = wrapk(kf[d], g.K[d]) - org[d];
+        for (int d = 0; d < NDIM; ++d)
+#pragma unroll
+            for (int j = 0; j < JL; ++j) mcr[d][j] = mci[d][j] = (R)0;
+        if (lane < nb) {
+            const int e = start + base + lane;
+            int loc[3] = {0, 0, 0};
+#pragma unroll
+            for (int d = 0; d < NDIM; ++d) {
+                const R t = p.s.t[d][e];
+                const int kf = first_tap(t, g.J[d]);
+                loc[d] = wrapk(kf, g.K[d]) - org[d];
+#pragma unroll
+                for (int j = 0; j < JL; ++j)
+                    if (JJ > 0 || j < g.J[d]) table_coef<R, CX>(g, d, t, kf + j, mcr[d][j], mci[d][j]);
+            }
+            mbase = ((loc[2] * Rd[1] + loc[1]) * Rd[0] + loc[0]) * LSP;
+            midx = p.s.idx[e];
+            if (p.apply_ph) mph = p.s.ph[e];
         }
-        R cr[NDIM][JMAX], ci[NDIM][JMAX];
+        for (int s0 = 0; s0 < nb; s0 += SW) {
+            const int src = s0 + slot;
+            R cr[NDIM][JL], ci[NDIM][JL];
 #pragma unroll
-        for (int d = 0; d < NDIM; ++d) {
+            for (int d = 0; d < NDIM; ++d) {
 #pragma unroll
-            for (int j = 0; j < JMAX; ++j) {
-                if (j < g.J[d]) {
-                    table_coef<R, CX>(g, d, t[d], kf[d] + j, cr[d][j], ci[d][j]);
-                } else {
+                for (int j = 0; j < JL; ++j) {
                     cr[d][j] = (R)0;
                     ci[d][j] = (R)0;
-                }
-            }
-        }
-        C acc = cmake<R>((R)0, (R)0);
-        if (NDIM == 1) {
-#pragma unroll
-            for (int j0 = 0; j0 < JMAX; ++j0) {
-                if (j0 < g.J[0]) {
-                    const int cell = loc[0] + j0;
-                    cfma<CX>(acc, cr[0][j0], ci[0][j0], S[(int64_t)cell * LSP + (coil ^ (cell & swz))]);
-                }
-            }
-        } else if (NDIM == 2) {
-#pragma unroll
-            for (int j1 = 0; j1 < JMAX; ++j1) {
-                if (j1 < g.J[1]) {
-                    const int base = (loc[1] + j1) * Rd[0] + loc[0];
-                    C row = cmake<R>((R)0, (R)0);
-#pragma unroll
-                    for (int j0 = 0; j0 < JMAX; ++j0) {
-                        if (j0 < g.J[0]) {
-                            const int cell = base + j0;
-                            cfma<CX>(row, cr[0][j0], ci[0][j0],
-                                     S[(int64_t)cell * LSP + (coil ^ (cell & swz))]);
-                        }
+                    if (JJ > 0 || j < g.J[d]) {
+                        cr[d][j] = __shfl_sync(0xffffffffu, mcr[d][j], src);
+                        if (CX) ci[d][j] = __shfl_sync(0xffffffffu, mci[d][j], src);
                     }
-                    cfma<CX>(acc, cr[NDIM > 1 ? 1 : 0][j1], ci[NDIM > 1 ? 1 : 0][j1], row);
                 }
             }
-        } else {
-#pragma unroll 1
-            for (int j2 = 0; j2 < JMAX; ++j2) {
-                if (j2 < g.J[2]) {
-                    C plane = cmake<R>((R)0, (R)0);
+            const int sbase = __shfl_sync(0xffffffffu, mbase, src) + coil;
+            const int idx = __shfl_sync(0xffffffffu, midx, src);
+            C ph;
+            ph.x = __shfl_sync(0xffffffffu, mph.x, src);
+            ph.y = __shfl_sync(0xffffffffu, mph.y, src);
+            if (src >= nb) continue;
+
+            C acc = cmake<R>((R)0, (R)0);
+            if (NDIM == 1) {
 #pragma unroll
-                    for (int j1 = 0; j1 < JMAX; ++j1) {
-                        if (j1 < g.J[1]) {
-                            const int base = ((loc[2] + j2) * Rd[1] + loc[1] + j1) * Rd[0] + loc[0];
-                            C row = cmake<R>((R)0, (R)0);
+                for (int j0 = 0; j0 < JL; ++j0)
+                    if (JJ > 0 || j0 < J0) cfma<CX>(acc, cr[0][j0], ci[0][j0], S[sbase + j0 * LSP]);
+            } else if (NDIM == 2) {
 #pragma unroll
-                            for (int j0 = 0; j0 < JMAX; ++j0) {
-                                if (j0 < g.J[0]) {
-                                    const int cell = base + j0;
-                                    cfma<CX>(row, cr[0][j0], ci[0][j0],
-                                             S[(int64_t)cell * LSP + (coil ^ (cell & swz))]);
-                                }
+                for (int j1 = 0; j1 < JL; ++j1) {
+                    if (JJ > 0 || j1 < J1) {
+                        const int rb = sbase + j1 * rowstride;
+                        C row = cmake<R>((R)0, (R)0);
+#pragma unroll
+                        for (int j0 = 0; j0 < JL; ++j0)
+                            if (JJ > 0 || j0 < J0) cfma<CX>(row, cr[0][j0], ci[0][j0], S[rb + j0 * LSP]);
+                        cfma<CX>(acc, cr[NDIM > 1 ? 1 : 0][j1], ci[NDIM > 1 ? 1 : 0][j1], row);
+                    }
+                }
+            } else {
+#pragma unroll
+                for (int j2 = 0; j2 < JL; ++j2) {
+                    if (JJ > 0 || j2 < J2) {
+                        C plane = cmake<R>((R)0, (R)0);
+#pragma unroll
+                        for (int j1 = 0; j1 < JL; ++j1) {
+                            if (JJ > 0 || j1 < J1) {
+                                const int rb = sbase + j2 * planestride + j1 * rowstride;
+                                C row = cmake<R>((R)0, (R)0);
+#pragma unroll
+                                for (int j0 = 0; j0 < JL; ++j0)
+                                    if (JJ > 0 || j0 < J0) cfma<CX>(row, cr[0][j0], ci[0][j0], S[rb + j0 * LSP]);
+                                cfma<CX>(plane, cr[NDIM > 1 ? 1 : 0][j1], ci[NDIM > 1 ? 1 : 0][j1], row);
                             }
-                            cfma<CX>(plane, cr[NDIM > 1 ? 1 : 0][j1], ci[NDIM > 1 ? 1 : 0][j1], row);
                         }
+                        cfma<CX>(acc, cr[NDIM > 2 ? 2 : 0][j2], ci[NDIM > 2 ? 2 : 0][j2], plane);
                     }
-                    cfma<CX>(acc, cr[NDIM > 2 ? 2 : 0][j2], ci[NDIM > 2 ? 2 : 0][j2], plane);
                 }
             }
-        }
-        if (coil < nc) {
-            if (p.apply_ph) acc = cmul(acc, p.s.ph[e]);
-            yb[p.s.idx[e]] = acc;
+            if (coil < nc) {
+                if (p.apply_ph) acc = cmul(acc, ph);
+                yb[idx] = acc;
+            }
         }
     }
 }
@@ -181,34 +213,74 @@ static cudaError_t ensure_smem(K kernel, size_t bytes) {
     return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
 }
 
-template <typename R, int NDIM, bool CX>
-static cudaError_t gather_dispatch(const GatherParams<R>& p, cudaStream_t s) {
+template <typename R, int NDIM, bool CX, int JJ, int LSC>
+static cudaError_t gather_launch(const GatherParams<R>& p, cudaStream_t s) {
     const size_t smem = gather_smem(p.g, p.ln);
-    cudaError_t e = ensure_smem(gather_kernel<R, NDIM, CX>, smem);
+    cudaError_t e = ensure_smem(gather_kernel<R, NDIM, CX, JJ, LSC>, smem);
     if (e != cudaSuccess) return e;
     dim3 grid(p.nitems, (p.coils + p.ln.LS - 1) / p.ln.LS);
-    gather_kernel<R, NDIM, CX><<<grid, GATHER_THREADS, smem, s>>>(p);
+    gather_kernel<R, NDIM, CX, JJ, LSC><<<grid, GATHER_THREADS, smem, s>>>(p);
     return cudaGetLastError();
+}
+
+// Kernel width shared by every axis, or 0.
+template <typename R>
+static int uniform_j(const Geom<R>& g) {
+    for (int d = 1; d < g.ndim; ++d)
+        if (g.J[d] != g.J[0]) return 0;
+    return g.J[0];
+}
+
+template <int NDIM>
+static cudaError_t gather_specialised(const GatherParams<float>& p, cudaStream_t s, bool* done) {
+    *done = true;
+    const int J = uniform_j(p.g);
+    const int LS = p.ln.LS;
+#define GBN_G(JV, LV) \
+    if (J == JV && LS == LV) return gather_launch<float, NDIM, false, JV, LV>(p, s);
+    GBN_G(6, 32) GBN_G(6, 8) GBN_G(6, 1) GBN_G(4, 32) GBN_G(4, 8) GBN_G(4, 1)
+#undef GBN_G
+    *done = false;
+    return cudaSuccess;
+}
+
+template <typename R>
+static cudaError_t launch_generic(const GatherParams<R>& p, cudaStream_t s) {
+    const bool cx = p.g.hi[0] != nullptr;
+    switch (p.g.ndim * 2 + (cx ? 1 : 0)) {
+        case 2: return gather_launch<R, 1, false, 0, 0>(p, s);
+        case 3: return gather_launch<R, 1, true, 0, 0>(p, s);
+        case 4: return gather_launch<R, 2, false, 0, 0>(p, s);
+        case 5: return gather_launch<R, 2, true, 0, 0>(p, s);
+        case 6: return gather_launch<R, 3, false, 0, 0>(p, s);
+        case 7: return gather_launch<R, 3, true, 0, 0>(p, s);
+    }
+    return cudaErrorInvalidValue;
+}
+
+static cudaError_t gather_any(const GatherParams<float>& p, cudaStream_t s) {
+    const bool cx = p.g.hi[0] != nullptr;
+    if (!cx && (p.g.ndim == 2 || p.g.ndim == 3)) {
+        bool done = false;
+        cudaError_t e = p.g.ndim == 2 ? gather_specialised<2>(p, s, &done) : gather_specialised<3>(p, s, &done);
+        if (done) return e;
+    }
+    return launch_generic<float>(p, s);
+}
+
+static cudaError_t gather_any(const GatherParams<double>& p, cudaStream_t s) {
+    return launch_generic<double>(p, s);
 }
 
 template <typename R>
 cudaError_t launch_gather(const GatherParams<R>& p, cudaStream_t s) {
     if (p.nitems == 0 || p.coils == 0) return cudaSuccess;
-    const bool cx = p.g.hi[0] != nullptr;
-    switch (p.g.ndim * 2 + (cx ? 1 : 0)) {
-        case 2: return gather_dispatch<R, 1, false>(p, s);
-        case 3: return gather_dispatch<R, 1, true>(p, s);
-        case 4: return gather_dispatch<R, 2, false>(p, s);
-        case 5: return gather_dispatch<R, 2, true>(p, s);
-        case 6: return gather_dispatch<R, 3, false>(p, s);
-        case 7: return gather_dispatch<R, 3, true>(p, s);
-    }
-    return cudaErrorInvalidValue;
+    return gather_any(p, s);
 }
 
-template size_t gather_smem<float>(const Geom<float>&, const Lanes&);
-template size_t gather_smem<double>(const Geom<double>&, const Lanes&);
 template cudaError_t launch_gather<float>(const GatherParams<float>&, cudaStream_t);
 template cudaError_t launch_gather<double>(const GatherParams<double>&, cudaStream_t);
+template size_t gather_smem<float>(const Geom<float>&, const Lanes&);
+template size_t gather_smem<double>(const Geom<double>&, const Lanes&);
 
 }  // namespace gbn

@@ -1,5 +1,5 @@
 // Internal declarations shared by the host planner (gbn_plan.cu) and the
-// device kernels (gbn_interp.cu, gbn_padcrop.cu, gbn_grad.cu).
+// device kernels (gbn_gather.cu, gbn_spread.cu, gbn_padcrop.cu, gbn_grad.cu).
 #pragma once
 
 #include <cuda_runtime.h>
@@ -10,18 +10,31 @@ namespace gbn {
 // Kernel width limit of the register-resident coefficient arrays.
 constexpr int JMAX = 8;
 
+// Spread register blocks: each warp of a spread CTA (at most 8 warps) owns
+// SB0 x SB1 x SB2 cells of its tile (16 accumulators per lane).
+template <int NDIM> struct SpreadBlock;
+template <> struct SpreadBlock<1> { static constexpr int B0 = 16, B1 = 1, B2 = 1; };
+template <> struct SpreadBlock<2> { static constexpr int B0 = 4, B1 = 4, B2 = 1; };
+template <> struct SpreadBlock<3> { static constexpr int B0 = 4, B1 = 4, B2 = 1; };
+// Zero-padded per-entry coefficient array length per axis: index
+// (block_origin - window_start) + (B - 1) + k, k < B, lies in [0, B + J + B - 2).
+constexpr int CPAD = 32;
+// Entries staged per spread chunk.
+constexpr int SPREAD_CHUNK_ENTRIES = 128;
+
 template <typename R> struct Cx;
 template <> struct Cx<float> { typedef float2 T; };
 template <> struct Cx<double> { typedef double2 T; };
 
-// Geometry in memory-axis order (axis 0 fastest).
+// Geometry in memory-axis order (axis 0 fastest) with the tiling of the
+// list being processed.
 template <typename R>
 struct Geom {
     int ndim;
     int N[3], K[3], J[3], T[3], nt[3];
     int L;
     int ncenter[3];          // floor(J*L/2): table index of t = 0
-    const R* hr[3];          // device tables (not shifted)
+    const R* hr[3];          // device tables (shifted past their zero padding)
     const R* hi[3];          // imaginary tables, nullptr for a real kernel
     int64_t Kprod, Nprod;
     R pbc[3];                // phase_before coefficient per memory axis
@@ -30,8 +43,7 @@ struct Geom {
 
 // Coil-lane layout of a CTA: LS lanes per sample (power of two <= 32),
 // SW = 32 / LS samples per warp.  Staged grid values for one cell occupy
-// LSP complex slots; for LS == 32 the slot is XOR-swizzled (swz = 31)
-// instead of padded.
+// LSP complex slots (LS + 1 for LS > 1: conflict-free transposed staging).
 struct Lanes {
     int LS, lsh, LSP, swz;
 };
@@ -42,6 +54,7 @@ struct SampleList {
     const R* t[3];                  // coordinate per memory axis, list order
     const int* idx;                 // sample index within its frame
     const typename Cx<R>::T* ph;    // per-sample phase (list order) or nullptr
+    const short4* ls;               // spread list: window start in tile coordinates
 };
 
 template <typename R>
@@ -72,7 +85,7 @@ struct SpreadParams {
     const int64_t* foff;
     const typename Cx<R>::T* y;
     typename Cx<R>::T* grid;
-    typename Cx<R>::T* scratch;     // [slot][tile cells][LS] partial sums
+    typename Cx<R>::T* scratch;     // [slot][chunk][LS][tile cells] partial sums
     int64_t tile_cells;             // T0*T1*T2
     int apply_pb;
     int apply_ph;
@@ -119,7 +132,7 @@ struct GradParams {
     Geom<R> g;
     const R* t[3];                  // coordinates, gather-list order
     const int* idx;                 // sample index of each list entry
-    const R* dh[3];                 // derivative tables (shifted by 2 like hr)
+    const R* dh[3];                 // derivative tables (shifted like hr)
     const typename Cx<R>::T* ph;    // sample phase, list order, or nullptr
     R phase_shift[3];               // s_d * gamma_d: d(phase)/d(tm_d) / i
     int64_t M;                      // list length (single frame)
@@ -141,6 +154,8 @@ template <typename R> cudaError_t launch_grad(const GradParams<R>& p, cudaStream
 // Shared-memory bytes needed by the gather / spread kernels for a lane layout.
 template <typename R> size_t gather_smem(const Geom<R>& g, const Lanes& ln);
 template <typename R> size_t spread_smem(const Geom<R>& g, const Lanes& ln);
+// Threads of a spread CTA for a tiling (one warp per register block).
+int spread_threads(int ndim, const int* T);
 
 cudaError_t launch_dtft(bool adjoint, int ndim, const int* Nd, const double* n_shift,
                         const double* omega, int64_t M, const double2* in, double2* out,

@@ -64,8 +64,8 @@ Lanes make_lanes(int ndim, int coils) {
     Lanes ln;
     ln.LS = std::min(lane_cap(ndim), next_pow2(std::max(coils, 1)));
     ln.lsh = ilog2(ln.LS);
-    ln.LSP = ln.LS == 32 ? 32 : (ln.LS == 1 ? 1 : ln.LS + 1);
-    ln.swz = ln.LS == 32 ? 31 : 0;
+    ln.LSP = ln.LS == 1 ? 1 : ln.LS + 1;
+    ln.swz = 0;
     return ln;
 }
 
@@ -109,8 +109,9 @@ struct gbn_plan {
     int F = 1;
     int64_t M_total = 0;
     std::vector<int64_t> foff;
-    int T[3] = {1, 1, 1}, nt[3] = {1, 1, 1};
-    int ntiles = 1;       // per frame
+    int Tg[3] = {1, 1, 1}, ntg[3] = {1, 1, 1};   // gather tiling
+    int Ts[3] = {1, 1, 1}, nts[3] = {1, 1, 1};   // spread tiling
+    int ntiles_g = 1, ntiles_s = 1;               // per frame
     int64_t Kprod = 1, Nprod = 1;
     int rsize = 4;        // sizeof(R)
     bool has_phase = false;
@@ -145,7 +146,7 @@ struct DeviceGuard {
 };
 
 template <typename R>
-Geom<R> make_geom(const gbn_plan* P) {
+Geom<R> make_geom(const gbn_plan* P, bool spread) {
     Geom<R> g;
     std::memset(&g, 0, sizeof(g));
     const gbn_geometry& G = P->geom;
@@ -159,8 +160,8 @@ Geom<R> make_geom(const gbn_plan* P) {
         g.N[d] = on ? G.Nd[d] : 1;
         g.K[d] = on ? G.Kd[d] : 1;
         g.J[d] = on ? G.Jd[d] : 1;
-        g.T[d] = P->T[d];
-        g.nt[d] = P->nt[d];
+        g.T[d] = spread ? P->Ts[d] : P->Tg[d];
+        g.nt[d] = spread ? P->nts[d] : P->ntg[d];
         g.ncenter[d] = on ? (int)std::floor((double)G.Jd[d] * (double)G.L / 2.0) : 0;
         g.pbc[d] = on ? (R)G.pb_coef[d] : (R)0;
         g.pbo[d] = on ? G.pb_order[d] : d;
@@ -181,36 +182,57 @@ Geom<R> make_geom(const gbn_plan* P) {
     return g;
 }
 
+// Sample-list buffer layout: window starts (spread list only), sample
+// phase (if any), one coordinate array per axis, sample index.  Every
+// section starts on a 16-byte boundary (double2 phases need it).
+inline size_t align16(size_t v) { return (v + 15) & ~(size_t)15; }
+
 template <typename R>
-SampleList<R> make_list(const gbn_plan* P, const DevBuf& buf, int64_t len) {
+struct ListLayout {
+    size_t ls = 0, ph = 0, t[3] = {0, 0, 0}, idx = 0, bytes = 0;
+    ListLayout(const gbn_plan* P, int64_t len, bool with_ls) {
+        size_t off = 0;
+        if (with_ls) {
+            ls = off;
+            off = align16(off + sizeof(short4) * (size_t)len);
+        }
+        if (P->has_phase) {
+            ph = off;
+            off = align16(off + sizeof(typename Cx<R>::T) * (size_t)len);
+        }
+        for (int d = 0; d < P->geom.ndim; ++d) {
+            t[d] = off;
+            off = align16(off + sizeof(R) * (size_t)len);
+        }
+        idx = off;
+        bytes = align16(off + sizeof(int) * (size_t)len) + 16;
+    }
+};
+
+template <typename R>
+SampleList<R> make_list(const gbn_plan* P, const DevBuf& buf, int64_t len, bool with_ls) {
     typedef typename Cx<R>::T C;
     SampleList<R> s;
     std::memset(&s, 0, sizeof(s));
-    char* b = reinterpret_cast<char*>(buf.p);
-    size_t off = 0;
-    const int ndim = P->geom.ndim;
-    // layout: ph [len] (if any), t[d] [len] each, idx [len]
-    if (P->has_phase) {
-        s.ph = reinterpret_cast<const C*>(b + off);
-        off += sizeof(C) * (size_t)len;
-    }
-    for (int d = 0; d < ndim; ++d) {
-        s.t[d] = reinterpret_cast<const R*>(b + off);
-        off += sizeof(R) * (size_t)len;
-    }
-    s.idx = reinterpret_cast<const int*>(b + off);
+    const char* b = reinterpret_cast<const char*>(buf.p);
+    const ListLayout<R> L(P, len, with_ls);
+    if (with_ls) s.ls = reinterpret_cast<const short4*>(b + L.ls);
+    if (P->has_phase) s.ph = reinterpret_cast<const C*>(b + L.ph);
+    for (int d = 0; d < P->geom.ndim; ++d) s.t[d] = reinterpret_cast<const R*>(b + L.t[d]);
+    s.idx = reinterpret_cast<const int*>(b + L.idx);
     return s;
 }
 
 template <typename R>
-size_t list_bytes(const gbn_plan* P, int64_t len) {
-    size_t b = (size_t)len * (sizeof(R) * P->geom.ndim + sizeof(int));
-    if (P->has_phase) b += (size_t)len * sizeof(typename Cx<R>::T);
-    return b + 64;
+size_t list_bytes(const gbn_plan* P, int64_t len, bool with_ls) {
+    return ListLayout<R>(P, len, with_ls).bytes;
 }
 
-// Choose tile edges: start from a per-dimension default and halve the
-// largest edge until the gather staging fits the shared-memory budget.
+// Gather tiling: start from a per-dimension default and halve the largest
+// edge until the staged tile + halo fits the shared-memory budget.
+// Spread tiling: a fixed number of register blocks per CTA (16 warps);
+// edges are multiples of the block edges and may exceed Kd (the cells past
+// Kd are never written).
 void choose_tiles(gbn_plan* P) {
     const gbn_geometry& G = P->geom;
     const int ndim = G.ndim;
@@ -219,7 +241,7 @@ void choose_tiles(gbn_plan* P) {
     if (ndim == 1) {
         T[0] = 256;
     } else if (ndim == 2) {
-        if (ln.LS >= 16) { T[0] = 16; T[1] = 16; }
+        if (ln.LS >= 16) { T[0] = 16; T[1] = 8; }
         else if (ln.LS >= 4) { T[0] = 32; T[1] = 16; }
         else { T[0] = 32; T[1] = 32; }
     } else {
@@ -240,10 +262,39 @@ void choose_tiles(gbn_plan* P) {
         T[dm] /= 2;
     }
     for (int d = 0; d < 3; ++d) {
-        P->T[d] = d < ndim ? std::max(1, std::min(T[d], G.Kd[d])) : 1;
-        P->nt[d] = d < ndim ? (G.Kd[d] + P->T[d] - 1) / P->T[d] : 1;
+        P->Tg[d] = d < ndim ? std::max(1, std::min(T[d], G.Kd[d])) : 1;
+        P->ntg[d] = d < ndim ? (G.Kd[d] + P->Tg[d] - 1) / P->Tg[d] : 1;
     }
-    P->ntiles = P->nt[0] * P->nt[1] * P->nt[2];
+    P->ntiles_g = P->ntg[0] * P->ntg[1] * P->ntg[2];
+    // spread: 8 register blocks (warps) per tile by default
+    int B[3] = {1, 1, 1}, S[3] = {1, 1, 1};
+    if (ndim == 1) { B[0] = SpreadBlock<1>::B0; S[0] = 8 * B[0]; }
+    else if (ndim == 2) { B[0] = SpreadBlock<2>::B0; B[1] = SpreadBlock<2>::B1; S[0] = 4 * B[0]; S[1] = 2 * B[1]; }
+    else {
+        B[0] = SpreadBlock<3>::B0; B[1] = SpreadBlock<3>::B1; B[2] = SpreadBlock<3>::B2;
+        S[0] = 2 * B[0]; S[1] = 2 * B[1]; S[2] = 2 * B[2];
+    }
+    for (int d = 0; d < ndim; ++d) {
+        if (G.stile[d] > 0) S[d] = std::max(B[d], (G.stile[d] / B[d]) * B[d]);
+        // no wider than the grid rounded up to whole blocks
+        const int kmax = ((G.Kd[d] + B[d] - 1) / B[d]) * B[d];
+        S[d] = std::min(S[d], kmax);
+    }
+    // at most 8 warps per CTA
+    for (int it = 0; it < 32; ++it) {
+        int w = 1;
+        for (int d = 0; d < ndim; ++d) w *= S[d] / B[d];
+        if (w <= 8) break;
+        int dm = 0;
+        for (int d = 1; d < ndim; ++d)
+            if (S[d] / B[d] > S[dm] / B[dm]) dm = d;
+        S[dm] = std::max(B[dm], ((S[dm] / 2) / B[dm]) * B[dm]);
+    }
+    for (int d = 0; d < 3; ++d) {
+        P->Ts[d] = d < ndim ? S[d] : 1;
+        P->nts[d] = d < ndim ? (G.Kd[d] + P->Ts[d] - 1) / P->Ts[d] : 1;
+    }
+    P->ntiles_s = P->nts[0] * P->nts[1] * P->nts[2];
 }
 
 template <typename R>
@@ -252,96 +303,114 @@ int build_lists(gbn_plan* P, const R* tm, const R* phase) {
     const gbn_geometry& G = P->geom;
     const int ndim = G.ndim;
     const int64_t Mt = P->M_total;
-    const int ntiles = P->ntiles;
-    const int64_t nbins = (int64_t)P->F * ntiles;
+    const int ntg = P->ntiles_g, nts = P->ntiles_s;
+    const int64_t nbins_g = (int64_t)P->F * ntg, nbins_s = (int64_t)P->F * nts;
 
+    // first tap of every sample, per axis (validated)
     std::vector<int> kf((size_t)Mt * ndim);
-    std::vector<int> gbin((size_t)Mt);
+    for (int64_t m = 0; m < Mt; ++m) {
+        for (int d = 0; d < ndim; ++d) {
+            const R t = tm[m * ndim + d];
+            if (!std::isfinite((double)t) || std::fabs((double)t) > TM_LIMIT)
+                return fail(GBN_ERR_INVALID, "sample coordinate is not finite or |tm| > 2^22");
+            kf[(size_t)m * ndim + d] = 1 + (int)std::floor((double)t - 0.5 * (double)G.Jd[d]);
+        }
+    }
+    auto wrap = [](int k, int K) {
+        int r = k % K;
+        return r < 0 ? r + K : r;
+    };
+    // ---- gather list: stable counting sort by the tile of the first tap ----
+    std::vector<int64_t> gbin((size_t)Mt);
     for (int f = 0; f < P->F; ++f) {
         for (int64_t m = P->foff[f]; m < P->foff[f + 1]; ++m) {
             int lin = 0, mul = 1;
             for (int d = 0; d < ndim; ++d) {
-                const R t = tm[m * ndim + d];
-                if (!std::isfinite((double)t) || std::fabs((double)t) > TM_LIMIT)
-                    return fail(GBN_ERR_INVALID, "sample coordinate is not finite or |tm| > 2^22");
-                const int k = 1 + (int)std::floor((double)t - 0.5 * (double)G.Jd[d]);
-                kf[(size_t)m * ndim + d] = k;
-                int home = k % G.Kd[d];
-                if (home < 0) home += G.Kd[d];
-                lin += (home / P->T[d]) * mul;
-                mul *= P->nt[d];
+                lin += (wrap(kf[(size_t)m * ndim + d], G.Kd[d]) / P->Tg[d]) * mul;
+                mul *= P->ntg[d];
             }
-            gbin[(size_t)m] = f * ntiles + lin;
+            gbin[(size_t)m] = (int64_t)f * ntg + lin;
         }
     }
-    // ---- gather list: stable counting sort by home tile -------------------
-    std::vector<int64_t> gcount((size_t)nbins + 1, 0);
+    std::vector<int64_t> gcount((size_t)nbins_g + 1, 0);
     for (int64_t m = 0; m < Mt; ++m) gcount[(size_t)gbin[m] + 1]++;
-    for (int64_t b = 0; b < nbins; ++b) gcount[b + 1] += gcount[b];
+    for (int64_t b = 0; b < nbins_g; ++b) gcount[b + 1] += gcount[b];
     std::vector<int64_t> gorder((size_t)Mt);
     {
         std::vector<int64_t> cur(gcount.begin(), gcount.end() - 1);
         for (int64_t m = 0; m < Mt; ++m) gorder[(size_t)cur[gbin[m]]++] = m;
     }
-    // ---- spread list: every tile a window touches ------------------------
-    // per axis: distinct tiles covered by the J window cells (wrap-aware)
-    auto axis_tiles = [&](int64_t m, int d, int* out) {
+    // ---- spread list: one entry per (tile, periodic image of the window)
+    // that touches the tile; the entry carries the window start in tile
+    // coordinates, so the kernel never wraps.
+    struct AxisHit { int tile; int ls; };
+    auto axis_hits = [&](int64_t m, int d, AxisHit* out) {
         int n = 0;
         for (int j = 0; j < G.Jd[d]; ++j) {
-            int c = (kf[(size_t)m * ndim + d] + j) % G.Kd[d];
-            if (c < 0) c += G.Kd[d];
-            const int tl = c / P->T[d];
+            const int c = wrap(kf[(size_t)m * ndim + d] + j, G.Kd[d]);
+            const int tl = c / P->Ts[d];
+            const int ls = c - tl * P->Ts[d] - j;
             bool seen = false;
-            for (int q = 0; q < n; ++q) seen = seen || out[q] == tl;
-            if (!seen) out[n++] = tl;
+            for (int q = 0; q < n; ++q) seen = seen || (out[q].tile == tl && out[q].ls == ls);
+            if (!seen) out[n++] = AxisHit{tl, ls};
         }
         return n;
     };
-    std::vector<int64_t> scount((size_t)nbins + 1, 0);
-    auto for_each_tile = [&](int64_t m, int f, auto&& fn) {
-        int tl[3][JMAX + 1];
-        int nt_[3] = {1, 1, 1};
-        for (int d = 0; d < 3; ++d) tl[d][0] = 0;
-        for (int d = 0; d < ndim; ++d) nt_[d] = axis_tiles(m, d, tl[d]);
-        for (int a2 = 0; a2 < nt_[2]; ++a2)
-            for (int a1 = 0; a1 < nt_[1]; ++a1)
-                for (int a0 = 0; a0 < nt_[0]; ++a0) {
-                    const int lin = tl[0][a0] + P->nt[0] * (tl[1][a1] + P->nt[1] * tl[2][a2]);
-                    fn(f * ntiles + lin);
+    auto for_each_entry = [&](int64_t m, int f, auto&& fn) {
+        AxisHit h[3][JMAX];
+        int nh[3] = {1, 1, 1};
+        for (int d = 0; d < 3; ++d) h[d][0] = AxisHit{0, 0};
+        for (int d = 0; d < ndim; ++d) nh[d] = axis_hits(m, d, h[d]);
+        for (int a2 = 0; a2 < nh[2]; ++a2)
+            for (int a1 = 0; a1 < nh[1]; ++a1)
+                for (int a0 = 0; a0 < nh[0]; ++a0) {
+                    const int lin = h[0][a0].tile + P->nts[0] * (h[1][a1].tile + P->nts[1] * h[2][a2].tile);
+                    short4 ls;
+                    ls.x = (short)h[0][a0].ls;
+                    ls.y = (short)h[1][a1].ls;
+                    ls.z = (short)h[2][a2].ls;
+                    ls.w = 0;
+                    fn((int64_t)f * nts + lin, ls);
                 }
     };
+    std::vector<int64_t> scount((size_t)nbins_s + 1, 0);
     for (int f = 0; f < P->F; ++f)
         for (int64_t m = P->foff[f]; m < P->foff[f + 1]; ++m)
-            for_each_tile(m, f, [&](int64_t b) { scount[(size_t)b + 1]++; });
-    for (int64_t b = 0; b < nbins; ++b) scount[b + 1] += scount[b];
-    const int64_t slen = scount[(size_t)nbins];
+            for_each_entry(m, f, [&](int64_t b, short4) { scount[(size_t)b + 1]++; });
+    for (int64_t b = 0; b < nbins_s; ++b) scount[b + 1] += scount[b];
+    const int64_t slen = scount[(size_t)nbins_s];
+    if (Mt > INT32_MAX || slen > INT32_MAX)
+        return fail(GBN_ERR_TOOLARGE, "more than 2^31 list entries");
     std::vector<int64_t> sorder((size_t)slen);
+    std::vector<short4> sls((size_t)slen);
     {
         std::vector<int64_t> cur(scount.begin(), scount.end() - 1);
         for (int f = 0; f < P->F; ++f)
             for (int64_t m = P->foff[f]; m < P->foff[f + 1]; ++m)
-                for_each_tile(m, f, [&](int64_t b) { sorder[(size_t)cur[b]++] = m; });
+                for_each_entry(m, f, [&](int64_t b, short4 ls) {
+                    const int64_t at = cur[b]++;
+                    sorder[(size_t)at] = m;
+                    sls[(size_t)at] = ls;
+                });
     }
     // ---- pack lists (SoA) -------------------------------------------------
-    auto pack = [&](const std::vector<int64_t>& order, DevBuf& dst, int64_t len) -> int {
-        const size_t bytes = list_bytes<R>(P, len);
+    auto pack = [&](const std::vector<int64_t>& order, const short4* ls, DevBuf& dst, int64_t len) -> int {
+        const ListLayout<R> L(P, len, ls != nullptr);
+        const size_t bytes = L.bytes;
         std::vector<char> host(bytes, 0);
-        size_t off = 0;
+        if (ls) std::memcpy(host.data() + L.ls, ls, sizeof(short4) * (size_t)len);
         if (P->has_phase) {
-            C* ph = reinterpret_cast<C*>(host.data() + off);
+            C* ph = reinterpret_cast<C*>(host.data() + L.ph);
             for (int64_t i = 0; i < len; ++i) {
                 ph[i].x = phase[2 * order[i]];
                 ph[i].y = phase[2 * order[i] + 1];
             }
-            off += sizeof(C) * (size_t)len;
         }
         for (int d = 0; d < ndim; ++d) {
-            R* t = reinterpret_cast<R*>(host.data() + off);
+            R* t = reinterpret_cast<R*>(host.data() + L.t[d]);
             for (int64_t i = 0; i < len; ++i) t[i] = tm[order[i] * ndim + d];
-            off += sizeof(R) * (size_t)len;
         }
-        int* idx = reinterpret_cast<int*>(host.data() + off);
-        // sample index within its frame
+        int* idx = reinterpret_cast<int*>(host.data() + L.idx);
         for (int64_t i = 0; i < len; ++i) {
             const int64_t m = order[i];
             const int f = (int)(std::upper_bound(P->foff.begin(), P->foff.end(), m) - P->foff.begin()) - 1;
@@ -353,9 +422,9 @@ int build_lists(gbn_plan* P, const R* tm, const R* phase) {
         if (e != cudaSuccess) return cuda_fail(e, "list upload");
         return GBN_OK;
     };
-    int rc = pack(gorder, P->glist, Mt);
+    int rc = pack(gorder, nullptr, P->glist, Mt);
     if (rc) return rc;
-    rc = pack(sorder, P->slist, slen);
+    rc = pack(sorder, sls.data(), P->slist, slen);
     if (rc) return rc;
     P->glen = Mt;
     P->slen = slen;
@@ -365,12 +434,15 @@ int build_lists(gbn_plan* P, const R* tm, const R* phase) {
     std::vector<Item> gi, si;
     std::vector<int4> rt;
     int slots = 0;
-    for (int64_t b = 0; b < nbins; ++b) {
-        const int f = (int)(b / ntiles), tile = (int)(b % ntiles);
+    for (int64_t b = 0; b < nbins_g; ++b) {
+        const int f = (int)(b / ntg), tile = (int)(b % ntg);
         const int64_t g0 = gcount[b], gn = gcount[b + 1] - g0;
-        for (int64_t s = 0; s < gn; s += GATHER_CHUNK)
-            gi.push_back({make_int4(f, tile, (int)(g0 + s), (int)std::min<int64_t>(GATHER_CHUNK, gn - s)),
+        for (int64_t q = 0; q < gn; q += GATHER_CHUNK)
+            gi.push_back({make_int4(f, tile, (int)(g0 + q), (int)std::min<int64_t>(GATHER_CHUNK, gn - q)),
                           make_int2(-1, 1)});
+    }
+    for (int64_t b = 0; b < nbins_s; ++b) {
+        const int f = (int)(b / nts), tile = (int)(b % nts);
         const int64_t s0 = scount[b], sn = scount[b + 1] - s0;
         const int parts = (int)std::max<int64_t>(1, (sn + SPREAD_CHUNK - 1) / SPREAD_CHUNK);
         if (parts == 1) {
@@ -386,8 +458,6 @@ int build_lists(gbn_plan* P, const R* tm, const R* phase) {
             slots += parts;
         }
     }
-    if (Mt > INT32_MAX || slen > INT32_MAX)
-        return fail(GBN_ERR_TOOLARGE, "more than 2^31 list entries");
     auto heavy_first = [](const Item& x, const Item& y) { return x.a.w > y.a.w; };
     std::stable_sort(gi.begin(), gi.end(), heavy_first);
     std::stable_sort(si.begin(), si.end(), heavy_first);
@@ -422,7 +492,7 @@ int build_lists(gbn_plan* P, const R* tm, const R* phase) {
 int ensure_scratch(gbn_plan* P, int coils) {
     const size_t csz = (size_t)2 * P->rsize;
     const Lanes ln = make_lanes(P->geom.ndim, coils);
-    const int64_t tile_cells = (int64_t)P->T[0] * P->T[1] * P->T[2];
+    const int64_t tile_cells = (int64_t)P->Ts[0] * P->Ts[1] * P->Ts[2];
     const int64_t chunks = (coils + ln.LS - 1) / ln.LS;
     // an upper bound for any lane count call_lanes may pick (halving LS
     // never increases chunks * LS)
@@ -484,10 +554,12 @@ int exec_fft(gbn_plan* P, cufftHandle h, void* in, void* out, int dir, cudaStrea
 // Coil lanes for a call: as many as the coil count asks for, halved until
 // the gather and spread shared memory fit the per-CTA limit with the plan's
 // tiles (a plan tiled for few coils still runs wide batches, in more chunks).
+// Both directions use the same lane count so the scratch bound holds.
 template <typename R>
-Lanes call_lanes(const gbn_plan* P, const Geom<R>& g, int coils) {
+Lanes call_lanes(const gbn_plan* P, int coils) {
+    const Geom<R> gg = make_geom<R>(P, false), gs = make_geom<R>(P, true);
     Lanes ln = make_lanes(P->geom.ndim, coils);
-    while (ln.LS > 1 && (gather_smem<R>(g, ln) > SMEM_LIMIT || spread_smem<R>(g, ln) > SMEM_LIMIT))
+    while (ln.LS > 1 && (gather_smem<R>(gg, ln) > SMEM_LIMIT || spread_smem<R>(gs, ln) > SMEM_LIMIT))
         ln = make_lanes(P->geom.ndim, ln.LS / 2);
     return ln;
 }
@@ -497,9 +569,9 @@ int run_gather(gbn_plan* P, const void* grid, void* y, int coils, bool phases, c
     typedef typename Cx<R>::T C;
     GatherParams<R> p;
     std::memset(&p, 0, sizeof(p));
-    p.g = make_geom<R>(P);
-    p.ln = call_lanes<R>(P, p.g, coils);
-    p.s = make_list<R>(P, P->glist, P->glen);
+    p.g = make_geom<R>(P, false);
+    p.ln = call_lanes<R>(P, coils);
+    p.s = make_list<R>(P, P->glist, P->glen, false);
     p.items = reinterpret_cast<const int4*>(P->gitems.p);
     p.nitems = P->n_gitems;
     p.coils = coils;
@@ -520,9 +592,9 @@ int run_spread(gbn_plan* P, const void* y, void* grid, int coils, bool phases, c
     if (rc) return rc;
     SpreadParams<R> p;
     std::memset(&p, 0, sizeof(p));
-    p.g = make_geom<R>(P);
-    p.ln = call_lanes<R>(P, p.g, coils);
-    p.s = make_list<R>(P, P->slist, P->slen);
+    p.g = make_geom<R>(P, true);
+    p.ln = call_lanes<R>(P, coils);
+    p.s = make_list<R>(P, P->slist, P->slen, true);
     p.items = reinterpret_cast<const int4*>(P->sitems.p);
     p.parts = reinterpret_cast<const int2*>(P->sparts.p);
     p.nitems = P->n_sitems;
@@ -531,7 +603,7 @@ int run_spread(gbn_plan* P, const void* y, void* grid, int coils, bool phases, c
     p.y = reinterpret_cast<const C*>(y);
     p.grid = reinterpret_cast<C*>(grid);
     p.scratch = reinterpret_cast<C*>(P->scratch.p);
-    p.tile_cells = (int64_t)P->T[0] * P->T[1] * P->T[2];
+    p.tile_cells = (int64_t)P->Ts[0] * P->Ts[1] * P->Ts[2];
     p.apply_pb = phases && P->geom.phasing == GBN_PHASING_REAL;
     p.apply_ph = phases && P->has_phase;
     GBN_CUDA(launch_spread<R>(p, s), "spread launch");
@@ -683,8 +755,8 @@ int run_grad(gbn_plan* P, const void* grid, const void* gy, const double* shift,
     typedef typename Cx<R>::T C;
     GradParams<R> p;
     std::memset(&p, 0, sizeof(p));
-    p.g = make_geom<R>(P);
-    const SampleList<R> L = make_list<R>(P, P->glist, P->glen);
+    p.g = make_geom<R>(P, false);
+    const SampleList<R> L = make_list<R>(P, P->glist, P->glen, false);
     const R* db = reinterpret_cast<const R*>(P->dtables.p);
     size_t off = 0;
     for (int d = 0; d < P->geom.ndim; ++d) {
@@ -892,7 +964,7 @@ int gbn_plan_stats(const gbn_plan* P, int64_t* o) {
     o[2] = P->n_rtiles;
     o[3] = P->glen;
     o[4] = P->slen;
-    o[5] = (int64_t)P->ntiles * P->F;
+    o[5] = (int64_t)P->ntiles_s * P->F;
     o[6] = (int64_t)(P->tables.bytes + P->sn.bytes + P->glist.bytes + P->slist.bytes + P->pad.bytes +
                      P->grid.bytes + P->scratch.bytes);
     o[7] = P->M_total;

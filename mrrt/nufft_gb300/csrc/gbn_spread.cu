@@ -2,16 +2,23 @@
 // grid.  Replaces the reference's scatters (serial per coil on the CPU,
 // mrrt/nufft/_extensions/c/nufft_table.template.c:144-531, 924-1206; global
 // atomicAdd per tap on the GPU, mrrt/nufft/cuda/jinja/table_*_adjoint.jinja)
-// with an "owner computes" decomposition:
+// with an "owner computes" decomposition and register accumulation:
 //
-// * a CTA owns one grid tile and one chunk of LS coils; it accumulates, in
-//   shared memory, the contributions that land in ITS tile from every sample
-//   whose window touches the tile (the planner lists halo samples in each
-//   tile they reach);
-// * each grid cell is then written exactly once, with conj(phase_before)
-//   applied -- no global atomics and no zero-fill of the grid;
-// * tiles too heavy for one CTA are split into parts whose partial tiles go
-//   to a scratch buffer and are summed in a fixed order by reduce_kernel.
+// * a CTA owns one grid tile and one chunk of LS coils; each of its warps
+//   owns a register block of SB0 x SB1 x SB2 = 16 (8 in 1-D) cells of the
+//   tile, held as accumulators in every lane (lane = (sample slot, coil));
+// * the planner lists every sample whose window touches the tile, with the
+//   window start in tile coordinates (one entry per periodic image that
+//   touches it, so the kernel never wraps);
+// * entries are staged by chunk in shared memory: zero-padded per-axis
+//   coefficient rows and the sample values for the LS coils;
+// * each warp ballots which staged entries touch its block and accumulates
+//   them in entry order: no atomics, no write conflicts, a fixed summation
+//   order (bitwise repeatable);
+// * sample slots of a warp are combined with warp shuffles and every grid
+//   cell is written exactly once, with conj(phase_before) applied.  Tiles
+//   too heavy for one CTA are split into parts whose partial tiles go to a
+//   scratch buffer and are summed in part order by reduce_kernel.
 #include <cuda_runtime.h>
 
 #include "gbn_device.cuh"
@@ -19,24 +26,57 @@
 
 namespace gbn {
 
-constexpr int SPREAD_THREADS = 256;
+__host__ __device__ constexpr int cpad_len(int B) { return ((2 * (B - 1) + JMAX + 3) / 4) * 4; }
 
-// ---------------------------------------------------------------------------
-// adjoint spread (owner computes)
-// ---------------------------------------------------------------------------
-template <typename R, int NDIM, bool CX>
-__global__ void __launch_bounds__(SPREAD_THREADS)
+template <int NDIM>
+struct SpreadLayout {
+    static constexpr int B0 = SpreadBlock<NDIM>::B0, B1 = SpreadBlock<NDIM>::B1, B2 = SpreadBlock<NDIM>::B2;
+    static constexpr int NB = B0 * B1 * B2;
+    static constexpr int P0 = cpad_len(B0), P1 = cpad_len(B1), P2 = cpad_len(B2);
+    static constexpr int PSUM = P0 + (NDIM > 1 ? P1 : 0) + (NDIM > 2 ? P2 : 0);
+    // row stride of the staged coefficient rows: odd, so the thread-per-entry
+    // staging stores fall in different banks
+    static constexpr int PSTR = PSUM + 1;
+};
+
+int spread_threads(int ndim, const int* T) {
+    int b[3];
+    if (ndim == 1) { b[0] = SpreadBlock<1>::B0; b[1] = b[2] = 1; }
+    else if (ndim == 2) { b[0] = SpreadBlock<2>::B0; b[1] = SpreadBlock<2>::B1; b[2] = 1; }
+    else { b[0] = SpreadBlock<3>::B0; b[1] = SpreadBlock<3>::B1; b[2] = SpreadBlock<3>::B2; }
+    int warps = 1;
+    for (int d = 0; d < ndim; ++d) warps *= T[d] / b[d];
+    return 32 * warps;
+}
+
+template <typename R, int NDIM, bool CX, int JJ, int LSC>
+__global__ void __launch_bounds__(256, 3)
 spread_kernel(const SpreadParams<R> p) {
     typedef typename Cx<R>::T C;
+    typedef SpreadLayout<NDIM> SL;
+    constexpr int B0 = SL::B0, B1 = SL::B1, B2 = SL::B2, NB = SL::NB;
+    constexpr int CH = SPREAD_CHUNK_ENTRIES;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    R* A = reinterpret_cast<R*>(smem_raw);
     const Geom<R>& g = p.g;
+
+    const int LS = LSC > 0 ? LSC : p.ln.LS;
+    const int lsh = LSC > 0 ? (LSC == 32 ? 5 : LSC == 16 ? 4 : LSC == 8 ? 3 : LSC == 4 ? 2 : LSC == 2 ? 1 : 0)
+                            : p.ln.lsh;
+    const int Jx = JJ > 0 ? JJ : g.J[0];
+    const int Jy = JJ > 0 ? JJ : g.J[NDIM > 1 ? 1 : 0];
+    const int Jz = JJ > 0 ? JJ : g.J[NDIM > 2 ? 2 : 0];
+    const int VS = LS + 1;
+    // shared layout: sample values [CH][VS], coefficient pairs [CH][PSTR],
+    // window starts [CH].  A coefficient pair holds (c, c) for a real kernel
+    // (so a packed multiply applies it to re and im at once) and
+    // (Re c, -Im c) = conj(c) for a complex kernel.
+    C* vbuf = reinterpret_cast<C*>(smem_raw);
+    C* cp = vbuf + CH * VS;
+    short4* sls = reinterpret_cast<short4*>(cp + CH * SL::PSTR);
 
     const int4 it = p.items[blockIdx.x];
     const int2 part = p.parts[blockIdx.x];
     const int f = it.x, tile = it.y, start = it.z, count = it.w;
-    const int LS = p.ln.LS, lsh = p.ln.lsh;
-    const int CS = 2 * LS + 1;  // floats per cell: re[LS], im[LS], pad
     const int c0 = blockIdx.y << lsh;
     const int nc = min(LS, p.coils - c0);
 
@@ -47,95 +87,148 @@ spread_kernel(const SpreadParams<R> p) {
         Td[d] = g.T[d];
         ext[d] = min(g.T[d], g.K[d] - org[d]);
     }
-    const int TT = Td[0] * Td[1] * Td[2];
 
-    for (int q = threadIdx.x; q < TT * CS; q += blockDim.x) A[q] = (R)0;
-    __syncthreads();
-
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int nwarps = blockDim.x >> 5;
+    const int tid = threadIdx.x;
+    const int warp = tid >> 5, lane = tid & 31;
     const int SW = 32 >> lsh;
     const int slot = lane >> lsh, coil = lane & (LS - 1);
+    // this warp's register block
+    const int nb0 = Td[0] / B0, nb1 = NDIM > 1 ? Td[1] / B1 : 1;
+    const int bo0 = (warp % nb0) * B0;
+    const int bo1 = NDIM > 1 ? ((warp / nb0) % nb1) * B1 : 0;
+    const int bo2 = NDIM > 2 ? (warp / (nb0 * nb1)) * B2 : 0;
+
+    C acc[NB];
+#pragma unroll
+    for (int q = 0; q < NB; ++q) acc[q] = cmake<R>((R)0, (R)0);
+
     const int64_t fo = p.foff[f];
     const int Mf = (int)(p.foff[f + 1] - fo);
-    const C* yb = p.y + fo * p.coils + (int64_t)(c0 + min(coil, nc - 1)) * Mf;
+    const C* yb = p.y + fo * p.coils + (int64_t)c0 * Mf;
 
-    for (int i0 = warp * SW; i0 < count; i0 += nwarps * SW) {
-        const int i = i0 + slot;
-        if (i >= count || coil >= nc) continue;
-        const int e = start + i;
-        C v = yb[p.s.idx[e]];
-        if (p.apply_ph) v = cmulc(v, p.s.ph[e]);
-        R t[3];
-        int kf[3];
-#pragma unroll
-        for (int d = 0; d < NDIM; ++d) {
-            t[d] = p.s.t[d][e];
-            kf[d] = first_tap(t[d], g.J[d]);
-        }
-        R cr[NDIM][JMAX], ci[NDIM][JMAX];
-        int lr[NDIM][JMAX];
-#pragma unroll
-        for (int d = 0; d < NDIM; ++d) {
-#pragma unroll
-            for (int j = 0; j < JMAX; ++j) {
-                lr[d][j] = -1;
-                cr[d][j] = (R)0;
-                ci[d][j] = (R)0;
-                if (j < g.J[d]) {
-                    const int l = wrapk(kf[d] + j, g.K[d]) - org[d];
-                    if (l >= 0 && l < ext[d]) {
-                        lr[d][j] = l;
-                        table_coef<R, CX>(g, d, t[d], kf[d] + j, cr[d][j], ci[d][j]);
-                    }
+    // zero padding of the coefficient rows: written once, the J coefficient
+    // slots of each row are overwritten per chunk
+    for (int q = tid; q < CH * SL::PSTR; q += blockDim.x) cp[q] = cmake<R>((R)0, (R)0);
+    const int Jsum = Jx + (NDIM > 1 ? Jy : 0) + (NDIM > 2 ? Jz : 0);
+
+    for (int cb = 0; cb < count; cb += CH) {
+        const int n = min(CH, count - cb);
+        const int e0 = start + cb;
+        __syncthreads();
+        // ---- stage: window starts and the J coefficients per axis --------------
+        for (int q = tid; q < n; q += blockDim.x) sls[q] = p.s.ls[e0 + q];
+        for (int q = tid; q < n * Jsum; q += blockDim.x) {
+            const int el = q / Jsum;
+            int j = q - el * Jsum;
+            int d = 0, slot0 = B0 - 1, Jd = Jx;
+            if (NDIM > 1 && j >= Jx) {
+                j -= Jx;
+                d = 1;
+                slot0 = SL::P0 + B1 - 1;
+                Jd = Jy;
+                if (NDIM > 2 && j >= Jy) {
+                    j -= Jy;
+                    d = 2;
+                    slot0 = SL::P0 + SL::P1 + B2 - 1;
+                    Jd = Jz;
                 }
             }
+            const R t = p.s.t[d][e0 + el];
+            R cr, ci;
+            table_coef<R, CX>(g, d, t, first_tap(t, Jd) + j, cr, ci);
+            cp[el * SL::PSTR + slot0 + j] = CX ? cmake<R>(cr, -ci) : cmake<R>(cr, cr);
         }
-        if (NDIM == 1) {
-#pragma unroll
-            for (int j0 = 0; j0 < JMAX; ++j0) {
-                if (lr[0][j0] >= 0) {
-                    const C w = cscale_conj<CX>(cr[0][j0], ci[0][j0], v);
-                    R* a = A + lr[0][j0] * CS + coil;
-                    atomicAdd(a, w.x);
-                    atomicAdd(a + LS, w.y);
-                }
-            }
-        } else if (NDIM == 2) {
-#pragma unroll
-            for (int j1 = 0; j1 < JMAX; ++j1) {
-                if (lr[NDIM > 1 ? 1 : 0][j1] >= 0) {
-                    const C v1 = cscale_conj<CX>(cr[NDIM > 1 ? 1 : 0][j1], ci[NDIM > 1 ? 1 : 0][j1], v);
-                    const int rowc = lr[NDIM > 1 ? 1 : 0][j1] * Td[0];
-#pragma unroll
-                    for (int j0 = 0; j0 < JMAX; ++j0) {
-                        if (lr[0][j0] >= 0) {
-                            const C w = cscale_conj<CX>(cr[0][j0], ci[0][j0], v1);
-                            R* a = A + (rowc + lr[0][j0]) * CS + coil;
-                            atomicAdd(a, w.x);
-                            atomicAdd(a + LS, w.y);
-                        }
-                    }
+        // ---- stage: sample values for the nc coils (entry-fastest loads) -------
+        if ((int)blockDim.x >= CH) {
+            const int el = tid % CH, cg = tid / CH, ng = blockDim.x / CH;
+            if (el < n) {
+                const int e = e0 + el;
+                const int ix = p.s.idx[e];
+                C ph = cmake<R>((R)1, (R)0);
+                if (p.apply_ph) ph = p.s.ph[e];
+                for (int c = cg; c < nc; c += ng) {
+                    C v = yb[(int64_t)c * Mf + ix];
+                    if (p.apply_ph) v = cmulc(v, ph);
+                    vbuf[el * VS + c] = v;
                 }
             }
         } else {
-#pragma unroll 1
-            for (int j2 = 0; j2 < JMAX; ++j2) {
-                if (lr[NDIM > 2 ? 2 : 0][j2] >= 0) {
-                    const C v2 = cscale_conj<CX>(cr[NDIM > 2 ? 2 : 0][j2], ci[NDIM > 2 ? 2 : 0][j2], v);
-                    const int pc = lr[NDIM > 2 ? 2 : 0][j2] * Td[1];
+            for (int el = tid; el < n; el += blockDim.x) {
+                const int e = e0 + el;
+                const int ix = p.s.idx[e];
+                C ph = cmake<R>((R)1, (R)0);
+                if (p.apply_ph) ph = p.s.ph[e];
+                for (int c = 0; c < nc; ++c) {
+                    C v = yb[(int64_t)c * Mf + ix];
+                    if (p.apply_ph) v = cmulc(v, ph);
+                    vbuf[el * VS + c] = v;
+                }
+            }
+        }
+        __syncthreads();
+        // ---- accumulate: each warp takes the entries touching its block --------
+        for (int gb = 0; gb < n; gb += 32) {
+            const int l = gb + lane;
+            bool hit = false;
+            if (l < n) {
+                const short4 s = sls[l];
+                hit = s.x < bo0 + B0 && s.x + Jx > bo0;
+                if (NDIM > 1) hit = hit && s.y < bo1 + B1 && s.y + Jy > bo1;
+                if (NDIM > 2) hit = hit && s.z < bo2 + B2 && s.z + Jz > bo2;
+            }
+            unsigned mask = __ballot_sync(0xffffffffu, hit);
+            while (mask) {
+                // slot k takes the k-th remaining hit, in entry order
+                int pos = -1;
+                for (int k = 0; k < SW && mask; ++k) {
+                    const int pk = __ffs(mask) - 1;
+                    mask &= mask - 1;
+                    if (k == slot) pos = pk;
+                }
+                if (pos >= 0 && coil < nc) {
+                    const int el = gb + pos;
+                    const short4 s = sls[el];
+                    const C v = vbuf[el * VS + coil];
+                    const C* row = cp + el * SL::PSTR;
+                    C a0[B0], a1[B1], a2[B2];
+                    const int i0 = bo0 - s.x + (B0 - 1);
 #pragma unroll
-                    for (int j1 = 0; j1 < JMAX; ++j1) {
-                        if (lr[NDIM > 1 ? 1 : 0][j1] >= 0) {
-                            const C v1 = cscale_conj<CX>(cr[NDIM > 1 ? 1 : 0][j1], ci[NDIM > 1 ? 1 : 0][j1], v2);
-                            const int rowc = (pc + lr[NDIM > 1 ? 1 : 0][j1]) * Td[0];
+                    for (int k = 0; k < B0; ++k) a0[k] = row[i0 + k];
+                    if (NDIM > 1) {
+                        const int i1 = SL::P0 + bo1 - s.y + (B1 - 1);
 #pragma unroll
-                            for (int j0 = 0; j0 < JMAX; ++j0) {
-                                if (lr[0][j0] >= 0) {
-                                    const C w = cscale_conj<CX>(cr[0][j0], ci[0][j0], v1);
-                                    R* a = A + (rowc + lr[0][j0]) * CS + coil;
-                                    atomicAdd(a, w.x);
-                                    atomicAdd(a + LS, w.y);
+                        for (int k = 0; k < B1; ++k) a1[k] = row[i1 + k];
+                    } else {
+                        a1[0] = cmake<R>((R)1, (R)0);   // neutral factor (real path reads .x only)
+                    }
+                    if (NDIM > 2) {
+                        const int i2 = SL::P0 + SL::P1 + bo2 - s.z + (B2 - 1);
+#pragma unroll
+                        for (int k = 0; k < B2; ++k) a2[k] = row[i2 + k];
+                    } else {
+                        a2[0] = cmake<R>((R)1, (R)0);
+                    }
+#pragma unroll
+                    for (int k2 = 0; k2 < B2; ++k2) {
+#pragma unroll
+                        for (int k1 = 0; k1 < B1; ++k1) {
+                            C tv;
+                            if (CX) {
+                                // conj(c2 c1) v, the pairs already hold conj
+                                const C w = cmul(a1[k1], a2[k2]);
+                                tv = cmul(w, v);
+                            } else {
+                                tv = rcmul(a1[k1].x * a2[k2].x, v);
+                            }
+#pragma unroll
+                            for (int k0 = 0; k0 < B0; ++k0) {
+                                const int q = (k2 * B1 + k1) * B0 + k0;
+                                if (CX) {
+                                    const C w0 = cmul(a0[k0], tv);
+                                    acc[q].x += w0.x;
+                                    acc[q].y += w0.y;
+                                } else {
+                                    acc[q] = rcfma(a0[k0].x, tv, acc[q]);
                                 }
                             }
                         }
@@ -144,35 +237,52 @@ spread_kernel(const SpreadParams<R> p) {
             }
         }
     }
-    __syncthreads();
 
-    // ---- flush: each owned cell written once ------------------------------
+    // ---- combine the sample slots of the warp ------------------------------
+    for (int off = LS; off < 32; off <<= 1) {
+#pragma unroll
+        for (int q = 0; q < NB; ++q) {
+            acc[q].x += __shfl_xor_sync(0xffffffffu, acc[q].x, off);
+            acc[q].y += __shfl_xor_sync(0xffffffffu, acc[q].y, off);
+        }
+    }
+
+    // ---- flush: each owned cell written once -------------------------------
+    // phase_before of the block's cells: lane q computes cell q (q < NB), the
+    // others read it by shuffle
+    C myph = cmake<R>((R)1, (R)0);
     const int slot_id = part.x;
-    for (int q = threadIdx.x; q < TT * nc; q += blockDim.x) {
-        const int c = q / TT;
-        const int cell = q - c * TT;
-        int r[3];
-        r[0] = cell % Td[0];
-        r[1] = (cell / Td[0]) % Td[1];
-        r[2] = cell / (Td[0] * Td[1]);
-        bool inside = true;
+    const bool direct = slot_id < 0;
+    if (direct && p.apply_pb && lane < NB) {
+        const int k0 = lane % B0, k1 = (lane / B0) % B1, k2 = lane / (B0 * B1);
+        int k[3] = {org[0] + bo0 + k0, org[1] + bo1 + k1, org[2] + bo2 + k2};
+        bool in = bo0 + k0 < ext[0];
+        if (NDIM > 1) in = in && bo1 + k1 < ext[1];
+        if (NDIM > 2) in = in && bo2 + k2 < ext[2];
+        if (in) myph = phase_before(g, k);
+    }
 #pragma unroll
-        for (int d = 0; d < NDIM; ++d) inside = inside && (r[d] < ext[d]);
-        if (!inside) continue;
-        C val = cmake<R>(A[cell * CS + c], A[cell * CS + LS + c]);
-        if (slot_id < 0) {
-            int k[3] = {0, 0, 0};
-            int64_t off = 0, stride = 1;
-#pragma unroll
-            for (int d = 0; d < NDIM; ++d) {
-                k[d] = org[d] + r[d];
-                off += (int64_t)k[d] * stride;
-                stride *= g.K[d];
-            }
-            if (p.apply_pb) val = cmulc(val, phase_before(g, k));
-            p.grid[((int64_t)f * p.coils + c0 + c) * g.Kprod + off] = val;
+    for (int q = 0; q < NB; ++q) {
+        const int k0 = q % B0, k1 = (q / B0) % B1, k2 = q / (B0 * B1);
+        R phr = (R)1, phi = (R)0;
+        if (direct && p.apply_pb) {
+            phr = __shfl_sync(0xffffffffu, myph.x, q);
+            phi = __shfl_sync(0xffffffffu, myph.y, q);
+        }
+        const int l0 = bo0 + k0, l1 = bo1 + k1, l2 = bo2 + k2;
+        bool in = l0 < ext[0];
+        if (NDIM > 1) in = in && l1 < ext[1];
+        if (NDIM > 2) in = in && l2 < ext[2];
+        if (!in || slot != 0 || coil >= nc) continue;
+        C val = acc[q];
+        if (direct) {
+            if (p.apply_pb) val = cmulc(val, cmake<R>(phr, phi));
+            const int64_t off = (int64_t)(org[0] + l0) +
+                                (int64_t)g.K[0] * ((int64_t)(org[1] + l1) + (int64_t)g.K[1] * (org[2] + l2));
+            p.grid[((int64_t)f * p.coils + c0 + coil) * g.Kprod + off] = val;
         } else {
-            p.scratch[(((int64_t)slot_id * gridDim.y + blockIdx.y) * LS + c) * p.tile_cells + cell] = val;
+            const int cell = l0 + Td[0] * (l1 + Td[1] * l2);
+            p.scratch[(((int64_t)slot_id * gridDim.y + blockIdx.y) * LS + coil) * p.tile_cells + cell] = val;
         }
     }
 }
@@ -227,9 +337,13 @@ __global__ void __launch_bounds__(256) reduce_kernel(const ReduceParams<R> p) {
 
 template <typename R>
 size_t spread_smem(const Geom<R>& g, const Lanes& ln) {
-    size_t cells = 1;
-    for (int d = 0; d < g.ndim; ++d) cells *= (size_t)g.T[d];
-    return cells * (size_t)(2 * ln.LS + 1) * sizeof(R);
+    int pstr = 0;
+    if (g.ndim == 1) pstr = SpreadLayout<1>::PSTR;
+    else if (g.ndim == 2) pstr = SpreadLayout<2>::PSTR;
+    else pstr = SpreadLayout<3>::PSTR;
+    const size_t CH = SPREAD_CHUNK_ENTRIES;
+    const size_t csz = sizeof(typename Cx<R>::T);
+    return CH * (size_t)(ln.LS + 1) * csz + CH * (size_t)pstr * csz + CH * sizeof(short4);
 }
 
 template <typename K>
@@ -238,29 +352,65 @@ static cudaError_t ensure_smem(K kernel, size_t bytes) {
     return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
 }
 
-template <typename R, int NDIM, bool CX>
-static cudaError_t spread_dispatch(const SpreadParams<R>& p, cudaStream_t s) {
+template <typename R, int NDIM, bool CX, int JJ, int LSC>
+static cudaError_t spread_launch(const SpreadParams<R>& p, cudaStream_t s) {
     const size_t smem = spread_smem(p.g, p.ln);
-    cudaError_t e = ensure_smem(spread_kernel<R, NDIM, CX>, smem);
+    cudaError_t e = ensure_smem(spread_kernel<R, NDIM, CX, JJ, LSC>, smem);
     if (e != cudaSuccess) return e;
+    const int threads = spread_threads(NDIM, p.g.T);
+    if (threads < 32 || threads > 256) return cudaErrorInvalidConfiguration;
     dim3 grid(p.nitems, (p.coils + p.ln.LS - 1) / p.ln.LS);
-    spread_kernel<R, NDIM, CX><<<grid, SPREAD_THREADS, smem, s>>>(p);
+    spread_kernel<R, NDIM, CX, JJ, LSC><<<grid, threads, smem, s>>>(p);
     return cudaGetLastError();
+}
+
+template <typename R>
+static cudaError_t spread_generic(const SpreadParams<R>& p, cudaStream_t s) {
+    const bool cx = p.g.hi[0] != nullptr;
+    switch (p.g.ndim * 2 + (cx ? 1 : 0)) {
+        case 2: return spread_launch<R, 1, false, 0, 0>(p, s);
+        case 3: return spread_launch<R, 1, true, 0, 0>(p, s);
+        case 4: return spread_launch<R, 2, false, 0, 0>(p, s);
+        case 5: return spread_launch<R, 2, true, 0, 0>(p, s);
+        case 6: return spread_launch<R, 3, false, 0, 0>(p, s);
+        case 7: return spread_launch<R, 3, true, 0, 0>(p, s);
+    }
+    return cudaErrorInvalidValue;
+}
+
+template <int NDIM>
+static cudaError_t spread_specialised(const SpreadParams<float>& p, cudaStream_t s, bool* done) {
+    *done = true;
+    int J = p.g.J[0];
+    for (int d = 1; d < p.g.ndim; ++d)
+        if (p.g.J[d] != J) J = 0;
+    const int LS = p.ln.LS;
+#define GBN_S(JV, LV) \
+    if (J == JV && LS == LV) return spread_launch<float, NDIM, false, JV, LV>(p, s);
+    GBN_S(6, 32) GBN_S(6, 8) GBN_S(6, 1) GBN_S(4, 32) GBN_S(4, 8) GBN_S(4, 1)
+#undef GBN_S
+    *done = false;
+    return cudaSuccess;
+}
+
+static cudaError_t spread_any(const SpreadParams<float>& p, cudaStream_t s) {
+    const bool cx = p.g.hi[0] != nullptr;
+    if (!cx && (p.g.ndim == 2 || p.g.ndim == 3)) {
+        bool done = false;
+        cudaError_t e = p.g.ndim == 2 ? spread_specialised<2>(p, s, &done) : spread_specialised<3>(p, s, &done);
+        if (done) return e;
+    }
+    return spread_generic<float>(p, s);
+}
+
+static cudaError_t spread_any(const SpreadParams<double>& p, cudaStream_t s) {
+    return spread_generic<double>(p, s);
 }
 
 template <typename R>
 cudaError_t launch_spread(const SpreadParams<R>& p, cudaStream_t s) {
     if (p.nitems == 0 || p.coils == 0) return cudaSuccess;
-    const bool cx = p.g.hi[0] != nullptr;
-    switch (p.g.ndim * 2 + (cx ? 1 : 0)) {
-        case 2: return spread_dispatch<R, 1, false>(p, s);
-        case 3: return spread_dispatch<R, 1, true>(p, s);
-        case 4: return spread_dispatch<R, 2, false>(p, s);
-        case 5: return spread_dispatch<R, 2, true>(p, s);
-        case 6: return spread_dispatch<R, 3, false>(p, s);
-        case 7: return spread_dispatch<R, 3, true>(p, s);
-    }
-    return cudaErrorInvalidValue;
+    return spread_any(p, s);
 }
 
 template <typename R>
