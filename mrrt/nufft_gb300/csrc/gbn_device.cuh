@@ -170,4 +170,17 @@ __device__ __forceinline__ void cfma(C& acc, R cr, R ci, C v) {
     }
 }
 
+
+// Asynchronous global -> shared copies (cp.async, cached in L1 and L2).
+// BYTES is 4, 8 or 16; both addresses must be aligned to BYTES.
+template <int BYTES>
+__device__ __forceinline__ void cp_async(void* smem, const void* gmem) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], %2;" ::"r"(s), "l"(gmem), "n"(BYTES) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+// Wait until every copy this thread issued has landed (bounded by memory
+// latency; no polling in this code).
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
 }  // namespace gbn

@@ -16,11 +16,9 @@ template <int NDIM> struct SpreadBlock;
 template <> struct SpreadBlock<1> { static constexpr int B0 = 16, B1 = 1, B2 = 1; };
 template <> struct SpreadBlock<2> { static constexpr int B0 = 4, B1 = 4, B2 = 1; };
 template <> struct SpreadBlock<3> { static constexpr int B0 = 4, B1 = 4, B2 = 1; };
-// Zero-padded per-entry coefficient array length per axis: index
-// (block_origin - window_start) + (B - 1) + k, k < B, lies in [0, B + J + B - 2).
-constexpr int CPAD = 32;
-// Entries staged per spread chunk.
-constexpr int SPREAD_CHUNK_ENTRIES = 128;
+// Entries staged per spread chunk (two chunks in flight: one accumulated
+// while the next is copied in).
+constexpr int SPREAD_CHUNK_ENTRIES = 64;
 
 template <typename R> struct Cx;
 template <> struct Cx<float> { typedef float2 T; };

@@ -66,13 +66,17 @@ spread_kernel(const SpreadParams<R> p) {
     const int Jy = JJ > 0 ? JJ : g.J[NDIM > 1 ? 1 : 0];
     const int Jz = JJ > 0 ? JJ : g.J[NDIM > 2 ? 2 : 0];
     const int VS = LS + 1;
-    // shared layout: sample values [CH][VS], coefficient pairs [CH][PSTR],
-    // window starts [CH].  A coefficient pair holds (c, c) for a real kernel
-    // (so a packed multiply applies it to re and im at once) and
-    // (Re c, -Im c) = conj(c) for a complex kernel.
+    // shared layout (two buffers for the copied-in chunk data, one for the
+    // coefficient rows computed from it):
+    //   vbuf[2][CH][VS]   sample values of the LS coils
+    //   cp[CH][PSTR]      coefficient pairs: (c, c) for a real kernel (a packed
+    //                     multiply applies c to re and im at once),
+    //                     (Re c, -Im c) = conj(c) for a complex kernel
+    //   tb[2][NDIM][CH]   coordinates, lsb[2][CH] window starts
     C* vbuf = reinterpret_cast<C*>(smem_raw);
-    C* cp = vbuf + CH * VS;
-    short4* sls = reinterpret_cast<short4*>(cp + CH * SL::PSTR);
+    C* cp = vbuf + 2 * CH * VS;
+    short4* lsb = reinterpret_cast<short4*>(cp + CH * SL::PSTR);
+    R* tb = reinterpret_cast<R*>(lsb + 2 * CH);
 
     const int4 it = p.items[blockIdx.x];
     const int2 part = p.parts[blockIdx.x];
@@ -111,13 +115,79 @@ spread_kernel(const SpreadParams<R> p) {
     for (int q = tid; q < CH * SL::PSTR; q += blockDim.x) cp[q] = cmake<R>((R)0, (R)0);
     const int Jsum = Jx + (NDIM > 1 ? Jy : 0) + (NDIM > 2 ? Jz : 0);
 
-    for (int cb = 0; cb < count; cb += CH) {
-        const int n = min(CH, count - cb);
-        const int e0 = start + cb;
+    // Copy-in assignment: each thread owns up to two entries of a chunk and
+    // the coils cg, cg + ng, ... of them.
+    const int nthr = blockDim.x;
+    const int ng = nthr >= CH ? nthr / CH : 1;
+    const int cg = nthr >= CH ? tid / CH : 0;
+    const int EPT = nthr >= CH ? 1 : CH / nthr;    // 1 or 2 (CTAs have >= 32 threads)
+    const int elo = nthr >= CH ? tid % CH : tid;
+    const int nchunks = (count + CH - 1) / CH;
+
+    // index and phase of this thread's entries, one chunk ahead of the copies
+    int nidx[2] = {0, 0};
+    C nph[2] = {cmake<R>((R)1, (R)0), cmake<R>((R)1, (R)0)};
+    C cph[2] = {cmake<R>((R)1, (R)0), cmake<R>((R)1, (R)0)};
+    auto load_meta = [&](int chunk) {
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+            const int el = elo + u * nthr;
+            const int n = min(CH, count - chunk * CH);
+            if (u < EPT && chunk < nchunks && el < n) {
+                const int e = start + chunk * CH + el;
+                nidx[u] = p.s.idx[e];
+                if (p.apply_ph) nph[u] = p.s.ph[e];
+            }
+        }
+    };
+    // issue the asynchronous copies of chunk `chunk` into buffer `b`
+    auto issue = [&](int chunk, int b) {
+        const int n = min(CH, count - chunk * CH);
+        const int e0 = start + chunk * CH;
+        C* vb = vbuf + b * CH * VS;
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+            const int el = elo + u * nthr;
+            if (u < EPT && el < n) {
+                const C* src = yb + nidx[u];
+                for (int c = cg; c < nc; c += ng) cp_async<sizeof(C)>(vb + el * VS + c, src + (int64_t)c * Mf);
+            }
+        }
+        for (int q = tid; q < n; q += nthr) {
+            cp_async<sizeof(short4)>(lsb + b * CH + q, p.s.ls + e0 + q);
+#pragma unroll
+            for (int d = 0; d < NDIM; ++d) cp_async<sizeof(R)>(tb + (b * NDIM + d) * CH + q, p.s.t[d] + e0 + q);
+        }
+        cp_async_commit();
+    };
+
+    if (nchunks > 0) {
+        load_meta(0);
+        issue(0, 0);
+#pragma unroll
+        for (int u = 0; u < 2; ++u) cph[u] = nph[u];
+        load_meta(1);
+    }
+
+    for (int k = 0; k < nchunks; ++k) {
+        const int b = k & 1;
+        const int n = min(CH, count - k * CH);
+        const C* vb = vbuf + b * CH * VS;
+        const short4* sls = lsb + b * CH;
+        // ---- chunk k has landed: apply conj(sample phase) to own values ------
+        cp_async_wait_all();
+        if (p.apply_ph) {
+            C* vw = vbuf + b * CH * VS;
+#pragma unroll
+            for (int u = 0; u < 2; ++u) {
+                const int el = elo + u * nthr;
+                if (u < EPT && el < n)
+                    for (int c = cg; c < nc; c += ng) vw[el * VS + c] = cmulc(vw[el * VS + c], cph[u]);
+            }
+        }
         __syncthreads();
-        // ---- stage: window starts and the J coefficients per axis --------------
-        for (int q = tid; q < n; q += blockDim.x) sls[q] = p.s.ls[e0 + q];
-        for (int q = tid; q < n * Jsum; q += blockDim.x) {
+        // ---- coefficient rows of chunk k (the J taps of each axis) -------------
+        for (int q = tid; q < n * Jsum; q += nthr) {
             const int el = q / Jsum;
             int j = q - el * Jsum;
             int d = 0, slot0 = B0 - 1, Jd = Jx;
@@ -133,37 +203,17 @@ spread_kernel(const SpreadParams<R> p) {
                     Jd = Jz;
                 }
             }
-            const R t = p.s.t[d][e0 + el];
+            const R t = tb[(b * NDIM + d) * CH + el];
             R cr, ci;
             table_coef<R, CX>(g, d, t, first_tap(t, Jd) + j, cr, ci);
             cp[el * SL::PSTR + slot0 + j] = CX ? cmake<R>(cr, -ci) : cmake<R>(cr, cr);
         }
-        // ---- stage: sample values for the nc coils (entry-fastest loads) -------
-        if ((int)blockDim.x >= CH) {
-            const int el = tid % CH, cg = tid / CH, ng = blockDim.x / CH;
-            if (el < n) {
-                const int e = e0 + el;
-                const int ix = p.s.idx[e];
-                C ph = cmake<R>((R)1, (R)0);
-                if (p.apply_ph) ph = p.s.ph[e];
-                for (int c = cg; c < nc; c += ng) {
-                    C v = yb[(int64_t)c * Mf + ix];
-                    if (p.apply_ph) v = cmulc(v, ph);
-                    vbuf[el * VS + c] = v;
-                }
-            }
-        } else {
-            for (int el = tid; el < n; el += blockDim.x) {
-                const int e = e0 + el;
-                const int ix = p.s.idx[e];
-                C ph = cmake<R>((R)1, (R)0);
-                if (p.apply_ph) ph = p.s.ph[e];
-                for (int c = 0; c < nc; ++c) {
-                    C v = yb[(int64_t)c * Mf + ix];
-                    if (p.apply_ph) v = cmulc(v, ph);
-                    vbuf[el * VS + c] = v;
-                }
-            }
+        // ---- copy-in of chunk k+1 overlaps with the accumulation of chunk k ----
+        if (k + 1 < nchunks) {
+            issue(k + 1, b ^ 1);
+#pragma unroll
+            for (int u = 0; u < 2; ++u) cph[u] = nph[u];
+            load_meta(k + 2);
         }
         __syncthreads();
         // ---- accumulate: each warp takes the entries touching its block --------
@@ -180,15 +230,15 @@ spread_kernel(const SpreadParams<R> p) {
             while (mask) {
                 // slot k takes the k-th remaining hit, in entry order
                 int pos = -1;
-                for (int k = 0; k < SW && mask; ++k) {
+                for (int kk = 0; kk < SW && mask; ++kk) {
                     const int pk = __ffs(mask) - 1;
                     mask &= mask - 1;
-                    if (k == slot) pos = pk;
+                    if (kk == slot) pos = pk;
                 }
                 if (pos >= 0 && coil < nc) {
                     const int el = gb + pos;
                     const short4 s = sls[el];
-                    const C v = vbuf[el * VS + coil];
+                    const C v = vb[el * VS + coil];
                     const C* row = cp + el * SL::PSTR;
                     C a0[B0], a1[B1], a2[B2];
                     const int i0 = bo0 - s.x + (B0 - 1);
@@ -343,7 +393,8 @@ size_t spread_smem(const Geom<R>& g, const Lanes& ln) {
     else pstr = SpreadLayout<3>::PSTR;
     const size_t CH = SPREAD_CHUNK_ENTRIES;
     const size_t csz = sizeof(typename Cx<R>::T);
-    return CH * (size_t)(ln.LS + 1) * csz + CH * (size_t)pstr * csz + CH * sizeof(short4);
+    return 2 * CH * (size_t)(ln.LS + 1) * csz + CH * (size_t)pstr * csz + 2 * CH * sizeof(short4) +
+           2 * (size_t)g.ndim * CH * sizeof(R);
 }
 
 template <typename K>
