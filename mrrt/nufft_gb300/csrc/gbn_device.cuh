@@ -183,4 +183,39 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 // latency; no polling in this code).
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
+
+// Element-wise pair operations: a * b and a * b + c on (re, im) pairs.
+__device__ __forceinline__ float2 pmul(float2 a, float2 b) { return fmul2(a, b); }
+__device__ __forceinline__ double2 pmul(double2 a, double2 b) { return make_double2(a.x * b.x, a.y * b.y); }
+__device__ __forceinline__ float2 pfma(float2 a, float2 b, float2 c) { return ffma2(a, b, c); }
+__device__ __forceinline__ double2 pfma(double2 a, double2 b, double2 c) {
+    return make_double2(fma(a.x, b.x, c.x), fma(a.y, b.y, c.y));
+}
+
+
+// acc += c * v with c given as a pair: (c, c) for a real kernel, the complex
+// coefficient (Re c, Im c) otherwise.
+template <bool CX, typename C>
+__device__ __forceinline__ void qfma(C& acc, C c, C v) {
+    if (CX) {
+        acc.x += c.x * v.x;
+        acc.y += c.x * v.y;
+        acc.x -= c.y * v.y;
+        acc.y += c.y * v.x;
+    } else {
+        acc = pfma(c, v, acc);
+    }
+}
+
+
+// Two adjacent complex values in one 16-byte store (single precision; the
+// address must be 16-byte aligned).  Double precision stores them singly.
+__device__ __forceinline__ void store_pair(float2* dst, float2 a, float2 b) {
+    *reinterpret_cast<float4*>(dst) = make_float4(a.x, a.y, b.x, b.y);
+}
+__device__ __forceinline__ void store_pair(double2* dst, double2 a, double2 b) {
+    dst[0] = a;
+    dst[1] = b;
+}
+
 }  // namespace gbn

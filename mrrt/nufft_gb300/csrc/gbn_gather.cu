@@ -148,6 +148,13 @@ gather_kernel(const GatherParams<R> p) {
                     }
                 }
             }
+            // coefficient pairs, built once per sample: (c, c) for a real kernel
+            // (packed multiply-add on re and im), (Re c, Im c) for a complex one
+            C q[NDIM][JL];
+#pragma unroll
+            for (int d = 0; d < NDIM; ++d)
+#pragma unroll
+                for (int j = 0; j < JL; ++j) q[d][j] = CX ? cmake<R>(cr[d][j], ci[d][j]) : cmake<R>(cr[d][j], cr[d][j]);
             const int sbase = __shfl_sync(0xffffffffu, mbase, src) + coil;
             const int idx = __shfl_sync(0xffffffffu, midx, src);
             C ph;
@@ -159,7 +166,7 @@ gather_kernel(const GatherParams<R> p) {
             if (NDIM == 1) {
 #pragma unroll
                 for (int j0 = 0; j0 < JL; ++j0)
-                    if (JJ > 0 || j0 < J0) cfma<CX>(acc, cr[0][j0], ci[0][j0], S[sbase + j0 * LSP]);
+                    if (JJ > 0 || j0 < J0) qfma<CX>(acc, q[0][j0], S[sbase + j0 * LSP]);
             } else if (NDIM == 2) {
 #pragma unroll
                 for (int j1 = 0; j1 < JL; ++j1) {
@@ -168,8 +175,8 @@ gather_kernel(const GatherParams<R> p) {
                         C row = cmake<R>((R)0, (R)0);
 #pragma unroll
                         for (int j0 = 0; j0 < JL; ++j0)
-                            if (JJ > 0 || j0 < J0) cfma<CX>(row, cr[0][j0], ci[0][j0], S[rb + j0 * LSP]);
-                        cfma<CX>(acc, cr[NDIM > 1 ? 1 : 0][j1], ci[NDIM > 1 ? 1 : 0][j1], row);
+                            if (JJ > 0 || j0 < J0) qfma<CX>(row, q[0][j0], S[rb + j0 * LSP]);
+                        qfma<CX>(acc, q[NDIM > 1 ? 1 : 0][j1], row);
                     }
                 }
             } else {
@@ -184,11 +191,11 @@ gather_kernel(const GatherParams<R> p) {
                                 C row = cmake<R>((R)0, (R)0);
 #pragma unroll
                                 for (int j0 = 0; j0 < JL; ++j0)
-                                    if (JJ > 0 || j0 < J0) cfma<CX>(row, cr[0][j0], ci[0][j0], S[rb + j0 * LSP]);
-                                cfma<CX>(plane, cr[NDIM > 1 ? 1 : 0][j1], ci[NDIM > 1 ? 1 : 0][j1], row);
+                                    if (JJ > 0 || j0 < J0) qfma<CX>(row, q[0][j0], S[rb + j0 * LSP]);
+                                qfma<CX>(plane, q[NDIM > 1 ? 1 : 0][j1], row);
                             }
                         }
-                        cfma<CX>(acc, cr[NDIM > 2 ? 2 : 0][j2], ci[NDIM > 2 ? 2 : 0][j2], plane);
+                        qfma<CX>(acc, q[NDIM > 2 ? 2 : 0][j2], plane);
                     }
                 }
             }

@@ -249,14 +249,14 @@ spread_kernel(const SpreadParams<R> p) {
 #pragma unroll
                         for (int k = 0; k < B1; ++k) a1[k] = row[i1 + k];
                     } else {
-                        a1[0] = cmake<R>((R)1, (R)0);   // neutral factor (real path reads .x only)
+                        a1[0] = CX ? cmake<R>((R)1, (R)0) : cmake<R>((R)1, (R)1);   // neutral factor
                     }
                     if (NDIM > 2) {
                         const int i2 = SL::P0 + SL::P1 + bo2 - s.z + (B2 - 1);
 #pragma unroll
                         for (int k = 0; k < B2; ++k) a2[k] = row[i2 + k];
                     } else {
-                        a2[0] = cmake<R>((R)1, (R)0);
+                        a2[0] = CX ? cmake<R>((R)1, (R)0) : cmake<R>((R)1, (R)1);
                     }
 #pragma unroll
                     for (int k2 = 0; k2 < B2; ++k2) {
@@ -268,7 +268,9 @@ spread_kernel(const SpreadParams<R> p) {
                                 const C w = cmul(a1[k1], a2[k2]);
                                 tv = cmul(w, v);
                             } else {
-                                tv = rcmul(a1[k1].x * a2[k2].x, v);
+                                // pairs (c, c): w12 = c1 c2 on both halves, tv = w12 v
+                                const C w12 = NDIM > 2 ? pmul(a1[k1], a2[k2]) : a1[k1];
+                                tv = pmul(w12, v);
                             }
 #pragma unroll
                             for (int k0 = 0; k0 < B0; ++k0) {
@@ -278,7 +280,7 @@ spread_kernel(const SpreadParams<R> p) {
                                     acc[q].x += w0.x;
                                     acc[q].y += w0.y;
                                 } else {
-                                    acc[q] = rcfma(a0[k0].x, tv, acc[q]);
+                                    acc[q] = pfma(a0[k0], tv, acc[q]);
                                 }
                             }
                         }
@@ -311,28 +313,45 @@ spread_kernel(const SpreadParams<R> p) {
         if (NDIM > 2) in = in && bo2 + k2 < ext[2];
         if (in) myph = phase_before(g, k);
     }
+    // cells are written in adjacent pairs: one 16-byte store when both are
+    // inside the grid and the address is aligned (single precision, even K0)
+    const bool vec_ok = sizeof(R) == 4 && (g.K[0] % 2) == 0;
 #pragma unroll
-    for (int q = 0; q < NB; ++q) {
+    for (int q = 0; q < NB; q += 2) {
         const int k0 = q % B0, k1 = (q / B0) % B1, k2 = q / (B0 * B1);
-        R phr = (R)1, phi = (R)0;
+        C ph0 = cmake<R>((R)1, (R)0), ph1 = cmake<R>((R)1, (R)0);
         if (direct && p.apply_pb) {
-            phr = __shfl_sync(0xffffffffu, myph.x, q);
-            phi = __shfl_sync(0xffffffffu, myph.y, q);
+            ph0.x = __shfl_sync(0xffffffffu, myph.x, q);
+            ph0.y = __shfl_sync(0xffffffffu, myph.y, q);
+            ph1.x = __shfl_sync(0xffffffffu, myph.x, q + 1);
+            ph1.y = __shfl_sync(0xffffffffu, myph.y, q + 1);
         }
         const int l0 = bo0 + k0, l1 = bo1 + k1, l2 = bo2 + k2;
-        bool in = l0 < ext[0];
-        if (NDIM > 1) in = in && l1 < ext[1];
-        if (NDIM > 2) in = in && l2 < ext[2];
-        if (!in || slot != 0 || coil >= nc) continue;
-        C val = acc[q];
+        bool row_in = true;
+        if (NDIM > 1) row_in = row_in && l1 < ext[1];
+        if (NDIM > 2) row_in = row_in && l2 < ext[2];
+        const bool in0 = row_in && l0 < ext[0], in1 = row_in && l0 + 1 < ext[0];
+        if (slot != 0 || coil >= nc) continue;
+        C v0 = acc[q], v1 = acc[q + 1];
         if (direct) {
-            if (p.apply_pb) val = cmulc(val, cmake<R>(phr, phi));
+            if (p.apply_pb) {
+                v0 = cmulc(v0, ph0);
+                v1 = cmulc(v1, ph1);
+            }
             const int64_t off = (int64_t)(org[0] + l0) +
                                 (int64_t)g.K[0] * ((int64_t)(org[1] + l1) + (int64_t)g.K[1] * (org[2] + l2));
-            p.grid[((int64_t)f * p.coils + c0 + coil) * g.Kprod + off] = val;
+            C* dst = p.grid + ((int64_t)f * p.coils + c0 + coil) * g.Kprod + off;
+            if (in0 && in1 && vec_ok) {
+                store_pair(dst, v0, v1);
+            } else {
+                if (in0) dst[0] = v0;
+                if (in1) dst[1] = v1;
+            }
         } else {
             const int cell = l0 + Td[0] * (l1 + Td[1] * l2);
-            p.scratch[(((int64_t)slot_id * gridDim.y + blockIdx.y) * LS + coil) * p.tile_cells + cell] = val;
+            C* dst = p.scratch + (((int64_t)slot_id * gridDim.y + blockIdx.y) * LS + coil) * p.tile_cells + cell;
+            if (in0) dst[0] = v0;
+            if (in1) dst[1] = v1;
         }
     }
 }
