@@ -19,6 +19,9 @@ Reported (one JSON line on rank 0):
              the host cores (bounded sample)
 ``--impl reference`` times the reference's CPU implementation instead (the
 reference itself where it is importable, else the oracle restatement).
+``--profile`` runs the same workload's kernels only (warm-up pairs, then
+``--steps`` batched pairs and one table gather and spread) without timing,
+parity or baselines: the command the kernel profiles are captured from.
 
 Multi-GPU: the coil batches are independent, so N GPUs run N replicas
 (weak scaling, no collective on the data path).
@@ -197,6 +200,25 @@ def run_reference(args, rank):
     print(json.dumps(line), flush=True)
 
 
+def max_over_ranks(t, world, device):
+    """The job's time for replicas: barrier, then the slowest rank's time
+    (all-reduce MAX), identical on every rank."""
+    if world <= 1:
+        return float(t)
+    import torch
+    import torch.distributed as dist
+
+    dist.barrier()
+    v = torch.tensor([float(t)], device=device, dtype=torch.float64)
+    dist.all_reduce(v, op=dist.ReduceOp.MAX)
+    return float(v.item())
+
+
+def job_value(units_per_rank, world, ms_per_step):
+    """Whole-job throughput: the units all ranks processed per second."""
+    return world * units_per_rank / (ms_per_step * 1e-3)
+
+
 def config_dict():
     w = WORKLOAD
     return {"workload": w["name"], "Nd": list(w["Nd"]), "Kd": list(w["Kd"]), "Jd": list(w["Jd"]),
@@ -266,11 +288,7 @@ def run_ours(args, rank, world):
     sampler = clock_sampler_start(clk_path) if rank == 0 else None
     t_batched = time_events(pair, args.steps, flush)
     torch.cuda.synchronize()
-    if world > 1:
-        torch.distributed.barrier()
-        t = torch.tensor([t_batched], device=dev, dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        t_batched = float(t.item())
+    t_batched = max_over_ranks(t_batched, world, dev)
 
     # ---- per-kernel timing for the roofline (same kernels, alone) -----------
     grid = torch.empty((C, w["Kd"][0] * w["Kd"][1]), dtype=torch.complex64, device=dev)
@@ -321,7 +339,7 @@ def run_ours(args, rank, world):
     if rank != 0:
         return
     ms_per_step = t_batched / args.steps
-    value = world * C / (ms_per_step * 1e-3)
+    value = job_value(C, world, ms_per_step)
     hbm, peak_kind = peaks()
     Kp = w["Kd"][0] * w["Kd"][1]
     B_alg = C * M * 8 + M * 2 * 4 + C * Kp * 8
@@ -355,13 +373,47 @@ def run_ours(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def run_profile(args):
+    """The workload's launches alone, for a profiler to capture."""
+    import torch
+
+    from mrrt.nufft_gb300 import NufftBase
+
+    w = WORKLOAD
+    C = w["coils"]
+    omega, x_f = build_inputs()
+    A = NufftBase(Nd=w["Nd"], omega=omega, Jd=w["Jd"], Kd=w["Kd"], Ld=w["L"], precision="single",
+                  on_gpu=True, max_coils=C)
+    P = A.plan
+    dev = torch.device("cuda", torch.cuda.current_device())
+    x_dev = torch.from_numpy(np.ascontiguousarray(np.moveaxis(x_f, -1, 0).transpose(0, 2, 1))).to(dev)
+    y_dev = torch.empty((C, A.M), dtype=torch.complex64, device=dev)
+    xa_dev = torch.empty_like(x_dev)
+    grid = torch.empty((C, w["Kd"][0] * w["Kd"][1]), dtype=torch.complex64, device=dev)
+    for _ in range(args.warmup + args.steps):
+        P.forward(x_dev, y_dev, C)
+        P.adjoint(y_dev, xa_dev, C)
+    grid.copy_(torch.randn_like(grid))
+    P.interp_forward(grid, y_dev, C)
+    P.interp_adjoint(y_dev, grid, C)
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_case": w["name"], "coils": C, "samples": A.M, "stats": P.stats()}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--profile", action="store_true", help="launch the workload's kernels only (no timing)")
     args = ap.parse_args()
+    if args.profile:
+        import torch
+
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        run_profile(args)
+        return
     args.warmup = max(3, args.warmup)
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
