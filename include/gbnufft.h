@@ -118,6 +118,30 @@ int gbn_interp_forward(gbn_plan* plan, const void* grid, void* y, int coils,
 int gbn_interp_adjoint(gbn_plan* plan, const void* y, void* grid, int coils,
                        void* stream);
 
+/* Capacity of the fixed scratch array behind gbn_interp_adjoint_noalloc. */
+#define GBN_NOALLOC_SCRATCH_BYTES (64u * 1024u * 1024u)
+
+/* Same result as gbn_interp_adjoint, for callers that must not allocate
+ * device memory during a call: a process whose device memory is committed
+ * up front to a fixed budget, or a pipeline that cannot let a cudaMalloc or
+ * cudaFree (which may synchronise the whole device) happen between its
+ * launches.  gbn_interp_adjoint grows a per-plan buffer for the partial sums
+ * of tiles split across CTAs; this variant keeps them in one statically
+ * sized array per device instead and never calls an allocator.
+ * No counterpart in the reference.
+ *   - Limit: the partial sums of one call must fit GBN_NOALLOC_SCRATCH_BYTES
+ *     (64 MiB); a larger request returns GBN_ERR_TOOLARGE before anything
+ *     is launched.  Fewer coils per call, or gbn_interp_adjoint, fit it.
+ *   - The first call on a device looks up that array's address (which can
+ *     also load the module holding it); make that first call before any
+ *     stream capture.
+ *   - Every plan on a device shares the one array: calls whose kernels can
+ *     overlap in time (unordered streams, or several host threads) race on
+ *     it and corrupt each other's results.  Order them on one stream or
+ *     synchronise between them.                                            */
+int gbn_interp_adjoint_noalloc(gbn_plan* plan, const void* y, void* grid,
+                               int coils, void* stream);
+
 /* Upload derivative tables dh/dt (host, length Jd[d]*L+1 per memory axis, plan
  * precision) used by gbn_grad_tm.  No counterpart in the reference.          */
 int gbn_plan_set_dtables(gbn_plan* plan, const void* const* dtab);

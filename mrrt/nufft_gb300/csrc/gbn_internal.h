@@ -155,6 +155,10 @@ template <typename R> size_t spread_smem(const Geom<R>& g, const Lanes& ln);
 // Threads of a spread CTA for a tiling (one warp per register block).
 int spread_threads(int ndim, const int* T);
 
+// Address and size of the fixed no-alloc scratch array on the current device
+// (gbn_noalloc.cu); looked up on the first request per device.
+cudaError_t noalloc_scratch(void** ptr, size_t* bytes);
+
 cudaError_t launch_dtft(bool adjoint, int ndim, const int* Nd, const double* n_shift,
                         const double* omega, int64_t M, const double2* in, double2* out,
                         int reps, cudaStream_t s);

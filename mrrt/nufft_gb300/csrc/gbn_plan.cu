@@ -624,6 +624,63 @@ int run_spread(gbn_plan* P, const void* y, void* grid, int coils, bool phases, c
     return GBN_OK;
 }
 
+// The spread of run_spread with the split-tile partial sums kept in the
+// fixed no-alloc array instead of the plan's scratch buffer.  Nothing here
+// allocates: the size check happens before any launch, and the array's
+// address comes from a per-device lookup done once.
+template <typename R>
+int run_spread_noalloc(gbn_plan* P, const void* y, void* grid, int coils, cudaStream_t s) {
+    typedef typename Cx<R>::T C;
+    void* scratch = nullptr;
+    size_t cap = 0;
+    cudaError_t e = noalloc_scratch(&scratch, &cap);
+    if (e != cudaSuccess) return cuda_fail(e, "no-alloc scratch address lookup");
+    const Lanes ln = call_lanes<R>(P, coils);
+    const int64_t tile_cells = (int64_t)P->Ts[0] * P->Ts[1] * P->Ts[2];
+    const int64_t chunks = (coils + ln.LS - 1) / ln.LS;
+    const int64_t need = (int64_t)P->n_slots * chunks * ln.LS * tile_cells * 2 * (int64_t)P->rsize;
+    if (need > (int64_t)cap) {
+        char msg[256];
+        std::snprintf(msg, sizeof(msg),
+                      "no-alloc adjoint needs %lld bytes of scratch for %d coils but its fixed array "
+                      "holds %zu; call with fewer coils or use gbn_interp_adjoint",
+                      (long long)need, coils, cap);
+        return fail(GBN_ERR_TOOLARGE, msg);
+    }
+    SpreadParams<R> p;
+    std::memset(&p, 0, sizeof(p));
+    p.g = make_geom<R>(P, true);
+    p.ln = ln;
+    p.s = make_list<R>(P, P->slist, P->slen, true);
+    p.items = reinterpret_cast<const int4*>(P->sitems.p);
+    p.parts = reinterpret_cast<const int2*>(P->sparts.p);
+    p.nitems = P->n_sitems;
+    p.coils = coils;
+    p.foff = reinterpret_cast<const int64_t*>(P->dfoff.p);
+    p.y = reinterpret_cast<const C*>(y);
+    p.grid = reinterpret_cast<C*>(grid);
+    p.scratch = reinterpret_cast<C*>(scratch);
+    p.tile_cells = tile_cells;
+    p.apply_pb = 0;
+    p.apply_ph = 0;
+    GBN_CUDA(launch_spread<R>(p, s), "no-alloc spread launch");
+    if (P->n_rtiles) {
+        ReduceParams<R> q;
+        std::memset(&q, 0, sizeof(q));
+        q.g = p.g;
+        q.ln = p.ln;
+        q.tiles = reinterpret_cast<const int4*>(P->rtiles.p);
+        q.ntiles = P->n_rtiles;
+        q.coils = coils;
+        q.scratch = p.scratch;
+        q.grid = p.grid;
+        q.tile_cells = p.tile_cells;
+        q.apply_pb = 0;
+        GBN_CUDA(launch_reduce<R>(q, s), "no-alloc reduce launch");
+    }
+    return GBN_OK;
+}
+
 template <typename R>
 int run_forward(gbn_plan* P, const void* x, void* y, int coils, cudaStream_t s) {
     int rc = ensure_buffers(P, coils);
@@ -889,6 +946,16 @@ int gbn_interp_adjoint(gbn_plan* P, const void* y, void* grid, int coils, void* 
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
     return P->dbl ? run_spread<double>(P, y, grid, coils, false, s)
                   : run_spread<float>(P, y, grid, coils, false, s);
+}
+
+int gbn_interp_adjoint_noalloc(gbn_plan* P, const void* y, void* grid, int coils, void* stream) {
+    int rc = check_call(P, y, grid, coils);
+    if (rc) return rc;
+    std::lock_guard<std::mutex> lk(P->mu);
+    DeviceGuard guard(P->device);
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    return P->dbl ? run_spread_noalloc<double>(P, y, grid, coils, s)
+                  : run_spread_noalloc<float>(P, y, grid, coils, s);
 }
 
 int gbn_forward_grid(gbn_plan* P, void** grid) {
