@@ -41,20 +41,40 @@ sys.path.insert(0, HERE)
 
 METRIC = "NUFFT fwd+adj pairs/s, batched vs plain per-call, at rel err ≤1e-4 vs FP64 NUDFT"
 UNIT = "coil-pairs/s"
-WORKLOAD = dict(name="2d-multicoil-radial", Nd=(256, 256), Kd=(512, 512), Jd=(6, 6), L=1024,
-                spokes=402, readout=512, coils=32)
+WORKLOADS = {
+    # the headline: one batched 32-coil operator vs 32 plain single-coil calls
+    "2d-multicoil-radial": dict(name="2d-multicoil-radial", kind="radial2d", Nd=(256, 256),
+                                Kd=(512, 512), Jd=(6, 6), L=1024, spokes=402, readout=512, coils=32),
+    # 3-D kooshball: interp3 gather and 3-D tiled spread
+    "3d-kooshball": dict(name="3d-kooshball", kind="koosh3d", Nd=(128, 128, 128), Kd=(256, 256, 256),
+                         Jd=(6, 6, 6), L=1024, spokes=12000, readout=256, coils=8),
+    # uneven dynamic series: every frame and coil in one launch per stage, CUDA graph, autotuned tiles
+    "series-2d": dict(name="series-2d", kind="series", Nd=(192, 192), Kd=(384, 384), Jd=(6, 6),
+                      L=1024, frames=64, readout=384, min_spokes=13, max_spokes=89, seed=4, coils=8),
+}
+WORKLOAD = WORKLOADS["2d-multicoil-radial"]
 
 
 def build_inputs():
-    from mrrt.nufft_gb300.trajectories import complex_image, gaussian_coil_maps, radial_2d
+    """(omega [M, d], x_f [*Nd, C] Fortran order) of a single-operator workload."""
+    from mrrt.nufft_gb300.trajectories import complex_image, gaussian_coil_maps, kooshball_3d, radial_2d
 
     w = WORKLOAD
-    omega = radial_2d(w["spokes"], w["readout"], golden=True)
+    if w["kind"] == "koosh3d":
+        omega = kooshball_3d(w["spokes"], w["readout"])
+    else:
+        omega = radial_2d(w["spokes"], w["readout"], golden=True)
     img = complex_image(w["Nd"], seed=0).astype(np.complex128)
     maps = gaussian_coil_maps(w["Nd"], w["coils"])
-    x = (maps * img[None]).astype(np.complex64)           # [C, N0, N1]
-    x_f = np.asfortranarray(np.moveaxis(x, 0, -1))        # [N0, N1, C] Fortran order
+    x = (maps * img[None]).astype(np.complex64)           # [C, *Nd]
+    x_f = np.asfortranarray(np.moveaxis(x, 0, -1))        # [*Nd, C] Fortran order
     return omega, x_f
+
+
+def plan_layout(x_f):
+    """[*Nd, C] Fortran order -> contiguous [C, N_{d-1}, ..., N_0] (the plan's layout)."""
+    nd = x_f.ndim - 1
+    return np.ascontiguousarray(np.moveaxis(x_f, -1, 0).transpose((0,) + tuple(range(nd, 0, -1))))
 
 
 def peaks():
@@ -121,25 +141,30 @@ def time_events(fn, steps, flush=None):
     return sum(s.elapsed_time(e) for s, e in zip(starts, ends))
 
 
-def cpu_baseline(omega, x_f, min_seconds=10.0, max_reps=50):
-    """Time the CPU table path (reference via its package where importable,
-    else the oracle restatement) on the full batched workload."""
-    w = WORKLOAD
-    kw = dict(Nd=w["Nd"], omega=omega, Jd=w["Jd"], Kd=w["Kd"], Ld=w["L"], precision="single")
-    kind = "port"
-    op = None
+def _cpu_operator(omega, w):
+    """The reference's CPU table operator where its package imports (this
+    container), else the oracle restatement (the GPU host); returns (op, kind)."""
+    kw = dict(Nd=w["Nd"], omega=omega, Jd=w["Jd"], Kd=w["Kd"], Ld=w["L"], precision="single",
+              mode="table")
     try:
         from oracle.ref_shim import load_reference, reference_available
 
         if reference_available():
-            op = load_reference().NufftBase(mode="table", **kw)
-            kind = "reference"
+            return load_reference().NufftBase(**kw), "reference"
     except Exception:
-        op = None
-    if op is None:
-        from oracle import oracle
+        pass
+    from oracle import oracle
 
-        op = oracle.OracleNufft(mode="table", **kw)
+    return oracle.OracleNufft(**kw), "port"
+
+
+def cpu_baseline(omega, x_f, min_seconds=10.0, max_reps=50):
+    """Time the CPU table path on the host cores: batched fwd+adj of the
+    coils in ``x_f`` (the full workload, or a bounded sample of its coils),
+    repeated for about ``min_seconds``."""
+    w = WORKLOAD
+    op, kind = _cpu_operator(omega, w)
+    coils = x_f.shape[-1]
     y = op.fft(x_f)
     op.adj(y)
     t0 = time.perf_counter()
@@ -153,48 +178,66 @@ def cpu_baseline(omega, x_f, min_seconds=10.0, max_reps=50):
             break
     per = el / reps
     return {
-        "value": w["coils"] / per,
+        "value": coils / per,
         "unit": UNIT,
         "cores": os.cpu_count(),
         "kind": kind,
-        "sample": "%d x batched fwd+adj of the full %d-coil workload (%.2f s each)" % (reps, w["coils"], per),
+        "sample": "%d x batched fwd+adj of %d of the workload's %d coils (%.2f s each)"
+                  % (reps, coils, w["coils"], per),
         "seconds_per_pair_batch": per,
     }
 
 
+def _cpu_sample_coils(w):
+    """Coils per CPU step: the full batch in 2-D; one coil of the 3-D volume
+    (a full 8-coil 3-D pair takes the CPU tens of seconds)."""
+    return 1 if len(w["Nd"]) == 3 else w["coils"]
+
+
 def run_reference(args, rank):
+    """The reference's CPU table path (or the oracle restatement of it where
+    the reference cannot be imported) on all host cores, same metric."""
     if rank != 0:
         return
-    omega, x_f = build_inputs()
     w = WORKLOAD
-    kw = dict(Nd=w["Nd"], omega=omega, Jd=w["Jd"], Kd=w["Kd"], Ld=w["L"], precision="single", mode="table")
-    kind = "port"
-    try:
-        from oracle.ref_shim import load_reference, reference_available
+    if w["kind"] == "series":
+        frames = _series_frames(w)[:4]
+        ops, kind = [], "port"
+        for om in frames:
+            op, kind = _cpu_operator(om, w)
+            ops.append(op)
+        xs = [np.asfortranarray(np.moveaxis(_series_images_host(w, f), 0, -1)) for f in range(len(frames))]
 
-        if reference_available():
-            op = load_reference().NufftBase(**kw)
-            kind = "reference"
-        else:
-            raise RuntimeError
-    except Exception:
-        from oracle import oracle
+        def step():
+            for op, x in zip(ops, xs):
+                op.adj(op.fft(x))
 
-        op = oracle.OracleNufft(**kw)
+        units = len(frames) * w["coils"]
+        sample = "each step: fwd+adj of frames 0-3 of the series, %d coils each, one operator per frame" % w["coils"]
+    else:
+        omega, x_f = build_inputs()
+        op, kind = _cpu_operator(omega, w)
+        xs = x_f[..., :_cpu_sample_coils(w)]
+
+        def step():
+            op.adj(op.fft(xs))
+
+        units = xs.shape[-1]
+        sample = "each step: batched fwd+adj of %d of the workload's %d coils" % (units, w["coils"])
     for _ in range(args.warmup):
-        op.adj(op.fft(x_f))
+        step()
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        op.adj(op.fft(x_f))
+        step()
     el = time.perf_counter() - t0
-    value = w["coils"] * args.steps / el
+    value = units * args.steps / el
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "complex64",
         "data": "synthetic", "config": config_dict(),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": os.cpu_count(), "kind": kind,
-                         "sample": "each step: batched fwd+adj of the full %d-coil workload" % w["coils"]},
+                         "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -219,12 +262,38 @@ def job_value(units_per_rank, world, ms_per_step):
     return world * units_per_rank / (ms_per_step * 1e-3)
 
 
-def config_dict():
+def config_dict(extra=None):
     w = WORKLOAD
-    return {"workload": w["name"], "Nd": list(w["Nd"]), "Kd": list(w["Kd"]), "Jd": list(w["Jd"]),
-            "L": w["L"], "trajectory": "golden-angle radial %dx%d" % (w["spokes"], w["readout"]),
-            "samples": w["spokes"] * w["readout"], "coils": w["coils"], "precision": "single",
-            "l2": "flushed between timed steps (256 MB write)", "parallelism": "replicas"}
+    cfg = {"workload": w["name"], "Nd": list(w["Nd"]), "Kd": list(w["Kd"]), "Jd": list(w["Jd"]),
+           "L": w["L"], "coils": w["coils"], "precision": "single",
+           "l2": "flushed between timed steps (256 MB write)", "parallelism": "replicas"}
+    if w["kind"] == "radial2d":
+        cfg["trajectory"] = "golden-angle radial %dx%d" % (w["spokes"], w["readout"])
+        cfg["samples"] = w["spokes"] * w["readout"]
+    elif w["kind"] == "koosh3d":
+        cfg["trajectory"] = "kooshball %d spokes x %d on a Fibonacci sphere" % (w["spokes"], w["readout"])
+        cfg["samples"] = w["spokes"] * w["readout"]
+    else:
+        cfg["trajectory"] = ("%d frames, U{%d..%d} golden-angle spokes (seed %d) x %d"
+                             % (w["frames"], w["min_spokes"], w["max_spokes"], w["seed"], w["readout"]))
+        cfg["frames"] = w["frames"]
+    if extra:
+        cfg.update(extra)
+    return cfg
+
+
+def _clock_path(rank):
+    out = os.path.join(HERE, "gpurun_out")
+    return os.path.join(out if os.path.isdir(out) else ".", "clocks_rank%d.csv" % rank)
+
+
+def _traffic(kernel):
+    """DRAM bytes per launch of a kernel from the committed ncu summary of the
+    default workload (read + write), or None."""
+    tp = os.path.join(HERE, "profiles", "traffic.json")
+    if WORKLOAD["name"] != "2d-multicoil-radial" or not os.path.exists(tp):
+        return None
+    return json.load(open(tp)).get(kernel)
 
 
 def run_ours(args, rank, world):
@@ -233,18 +302,21 @@ def run_ours(args, rank, world):
     from mrrt.nufft_gb300 import NufftBase, dtft
     from oracle import oracle
 
+    if WORKLOAD["kind"] == "series":
+        return run_series(args, rank, world)
     dev = torch.device("cuda", torch.cuda.current_device())
     w = WORKLOAD
     C = w["coils"]
+    nd = len(w["Nd"])
     omega, x_f = build_inputs()
     kw = dict(Nd=w["Nd"], omega=omega, Jd=w["Jd"], Kd=w["Kd"], Ld=w["L"], precision="single")
     A = NufftBase(on_gpu=True, max_coils=C, **kw)
     A1 = NufftBase(on_gpu=True, max_coils=1, **kw)
     P, P1 = A.plan, A1.plan
     M = A.M
-    N0, N1 = w["Nd"]
-    # device-resident inputs in the plan layout [coil][N1][N0]
-    x_dev = torch.from_numpy(np.ascontiguousarray(np.moveaxis(x_f, -1, 0).transpose(0, 2, 1))).to(dev)
+    Kp = int(np.prod(w["Kd"]))
+    # device-resident inputs in the plan layout [coil][N_{d-1}]...[N_0]
+    x_dev = torch.from_numpy(plan_layout(x_f)).to(dev)
     y_dev = torch.empty((C, M), dtype=torch.complex64, device=dev)
     xa_dev = torch.empty_like(x_dev)
     flush_buf = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
@@ -256,23 +328,24 @@ def run_ours(args, rank, world):
         P.forward(x_dev, y_dev, C)
         P.adjoint(y_dev, xa_dev, C)
 
-    # ---- parity (untimed): coil 0 vs the oracle; error vs the exact NUDFT ----
+    # ---- parity (untimed): first coils vs the oracle; error vs the exact NUDFT
     pair()
     torch.cuda.synchronize()
     parity = {}
     if rank == 0:
         B = oracle.OracleNufft(**kw)
-        x0 = x_f[..., :2]
-        y_or = B.fft(x0)
-        y_gpu = y_dev[:2].cpu().numpy().T
-        parity["fwd_rel_err_vs_oracle"] = oracle.rel_l2(y_gpu, y_or)
-        xa_or = B.adj(y_gpu)
-        xa_gpu = xa_dev[:2].cpu().numpy().transpose(2, 1, 0)
-        parity["adj_rel_err_vs_oracle"] = oracle.rel_l2(xa_gpu, xa_or)
-        rows = np.random.default_rng(0).choice(M, 4096, replace=False)
+        npar = 2 if nd < 3 else 1
+        y_or = B.fft(x_f[..., :npar])
+        y_gpu = y_dev[:npar].cpu().numpy().T
+        parity["fwd_rel_err_vs_oracle"] = oracle.rel_l2(y_gpu.reshape(y_or.shape), y_or)
+        xa_or = B.adj(y_gpu.reshape(y_or.shape))
+        xa_gpu = xa_dev[:npar].cpu().numpy().transpose(tuple(range(nd, -1, -1)))
+        parity["adj_rel_err_vs_oracle"] = oracle.rel_l2(xa_gpu.reshape(xa_or.shape), xa_or)
+        rows = np.random.default_rng(0).choice(M, 4096 if nd < 3 else 1024, replace=False)
         y_ex = dtft(x_f[..., 0].astype(np.complex128), omega[rows], shape=w["Nd"])
+        y_or0 = y_or.reshape(M, -1)[:, 0]
         parity["fwd_rel_err_vs_fp64_nudft"] = oracle.rel_l2(y_gpu[rows, 0], y_ex)
-        parity["oracle_fwd_rel_err_vs_fp64_nudft"] = oracle.rel_l2(y_or[rows, 0], y_ex)
+        parity["oracle_fwd_rel_err_vs_fp64_nudft"] = oracle.rel_l2(y_or0[rows], y_ex)
 
     stats = P.stats()
     launches_per_step = 2 + 2 + (1 if stats["split_tiles"] > 0 else 0)
@@ -283,15 +356,13 @@ def run_ours(args, rank, world):
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
-    clk_path = os.path.join(HERE, "gpurun_out" if os.path.isdir(os.path.join(HERE, "gpurun_out")) else ".",
-                            "clocks_rank%d.csv" % rank)
-    sampler = clock_sampler_start(clk_path) if rank == 0 else None
+    sampler = clock_sampler_start(_clock_path(rank)) if rank == 0 else None
     t_batched = time_events(pair, args.steps, flush)
     torch.cuda.synchronize()
     t_batched = max_over_ranks(t_batched, world, dev)
 
     # ---- per-kernel timing for the roofline (same kernels, alone) -----------
-    grid = torch.empty((C, w["Kd"][0] * w["Kd"][1]), dtype=torch.complex64, device=dev)
+    grid = torch.empty((C, Kp), dtype=torch.complex64, device=dev)
 
     def spread():
         P.interp_adjoint(y_dev, grid, C)
@@ -304,7 +375,7 @@ def run_ours(args, rank, world):
         gather()
     t_spread = time_events(spread, args.steps, flush) / args.steps
     t_gather = time_events(gather, args.steps, flush) / args.steps
-    clocks = clock_sampler_stop(sampler, clk_path, dev.index) if rank == 0 else None
+    clocks = clock_sampler_stop(sampler, _clock_path(rank), dev.index) if rank == 0 else None
 
     # ---- plain per-call loop on the same GPU --------------------------------
     x1 = [x_dev[c:c + 1].contiguous() for c in range(C)]
@@ -322,6 +393,7 @@ def run_ours(args, rank, world):
     t_percall = time_events(per_call, per_steps, flush) / per_steps
 
     # ---- end to end through the public API with host buffers ----------------
+    del x1, y1, xa1, grid
     Ah = NufftBase(on_gpu=False, max_coils=C, **kw)
     for _ in range(2):
         Ah.adj(Ah.fft(x_f))
@@ -341,26 +413,22 @@ def run_ours(args, rank, world):
     ms_per_step = t_batched / args.steps
     value = job_value(C, world, ms_per_step)
     hbm, peak_kind = peaks()
-    Kp = w["Kd"][0] * w["Kd"][1]
-    B_alg = C * M * 8 + M * 2 * 4 + C * Kp * 8
+    B_alg = C * M * 8 + M * nd * 4 + C * Kp * 8
     dominant = "spread" if t_spread >= t_gather else "gather"
     t_dom = max(t_spread, t_gather)
     achieved = B_alg / (t_dom * 1e-3) / 1e9
-    traffic = None
-    tp = os.path.join(HERE, "profiles", "traffic.json")
-    if os.path.exists(tp):
-        traffic = json.load(open(tp)).get(dominant)
-    cpu = cpu_baseline(omega, x_f)
+    cpu = cpu_baseline(omega, x_f[..., :_cpu_sample_coils(w)])
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "complex64", "data": "synthetic",
         "config": config_dict(),
-        "per_call": {"value": C / (t_percall * 1e-3), "unit": UNIT, "ms_per_32_coil_pairs": t_percall,
+        "per_call": {"value": C / (t_percall * 1e-3), "unit": UNIT, "ms_per_step": t_percall,
+                     "calls_per_step": 2 * C,
                      "batched_over_per_call": (C / (ms_per_step * 1e-3)) / (C / (t_percall * 1e-3))},
         "roofline": {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": hbm,
                      "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / hbm,
-                     "traffic": traffic, "algorithmic_bytes": B_alg,
+                     "traffic": _traffic(dominant), "algorithmic_bytes": B_alg,
                      "kernel_ms": {"spread": t_spread, "gather": t_gather}},
         "cpu_baseline": {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")},
         "e2e": {"value": C / t_e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
@@ -373,6 +441,204 @@ def run_ours(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def _series_frames(w):
+    from mrrt.nufft_gb300.trajectories import uneven_series_2d
+
+    return uneven_series_2d(w["frames"], w["readout"], min_spokes=w["min_spokes"],
+                            max_spokes=w["max_spokes"], seed=w["seed"])
+
+
+def _series_images_host(w, f):
+    """Frame f's coil images [C, *Nd] (complex64): a seeded N(0,1) image per
+    frame times the Gaussian coil maps."""
+    from mrrt.nufft_gb300.trajectories import complex_image, gaussian_coil_maps
+
+    img = complex_image(w["Nd"], seed=100 + f).astype(np.complex128)
+    return (gaussian_coil_maps(w["Nd"], w["coils"]) * img[None]).astype(np.complex64)
+
+
+def run_series(args, rank, world):
+    """The uneven dynamic series: all frames and coils in one plan (one launch
+    per stage), tiles from the autotuner, steps replayed from CUDA graphs;
+    against one plain single-coil call per frame and coil."""
+    import torch
+
+    from mrrt.nufft_gb300 import NufftBase, dtft
+    from mrrt.nufft_gb300.autotune import tune_series
+    from mrrt.nufft_gb300.series import NufftSeries
+    from oracle import oracle
+
+    dev = torch.device("cuda", torch.cuda.current_device())
+    w = WORKLOAD
+    C, F = w["coils"], w["frames"]
+    oms = _series_frames(w)
+    tile, stile, report = tune_series(w["Nd"], oms, Jd=w["Jd"], Kd=w["Kd"], Ld=w["L"], coils=C, reps=3)
+    S = NufftSeries(w["Nd"], oms, Jd=w["Jd"], Kd=w["Kd"], Ld=w["L"], coils=C, tile=tile, stile=stile)
+    x_host = np.stack([plan_layout(np.asfortranarray(np.moveaxis(_series_images_host(w, f), 0, -1)))
+                       for f in range(F)])                     # [F, C, N1, N0]
+    x_dev = torch.from_numpy(x_host).to(dev)
+    flush_buf = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    def flush():
+        flush_buf.fill_(1.0)
+
+    S.capture()
+    S.x_static.copy_(x_dev)
+
+    def pair_graph():
+        S.replay_forward()
+        S.replay_adjoint()
+
+    y_eager = S.forward(x_dev)
+    xa_eager = S.adjoint(y_eager)
+    torch.cuda.synchronize()
+
+    # ---- parity (untimed): frames vs the oracle, one frame vs the FP64 NUDFT
+    parity = {}
+    if rank == 0:
+        ys = S.split_samples(y_eager)
+        errs_f, errs_a = [], []
+        for f in (0, F // 2, F - 1):
+            B = oracle.OracleNufft(Nd=w["Nd"], omega=oms[f], Jd=w["Jd"], Kd=w["Kd"], Ld=w["L"],
+                                   precision="single")
+            xf = np.asfortranarray(np.moveaxis(_series_images_host(w, f), 0, -1)[..., :2])
+            y_or = B.fft(xf)
+            y_gpu = ys[f][:2].cpu().numpy().T
+            errs_f.append(oracle.rel_l2(y_gpu, y_or))
+            xa_or = B.adj(y_gpu)
+            errs_a.append(oracle.rel_l2(xa_eager[f, :2].cpu().numpy().transpose(2, 1, 0), xa_or))
+        parity["fwd_rel_err_vs_oracle_max_of_3_frames"] = max(errs_f)
+        parity["adj_rel_err_vs_oracle_max_of_3_frames"] = max(errs_a)
+        f = 17
+        rows = np.random.default_rng(0).choice(oms[f].shape[0], 2048, replace=False)
+        x17 = _series_images_host(w, f)[0].astype(np.complex128)
+        y_ex = dtft(x17, oms[f][rows], shape=w["Nd"])
+        parity["fwd_rel_err_vs_fp64_nudft_frame17"] = oracle.rel_l2(ys[f][0].cpu().numpy()[rows], y_ex)
+
+    stats = S.plan.stats()
+    launches_per_step = 2 + 2 + (1 if stats["split_tiles"] > 0 else 0)
+
+    # ---- batched series from CUDA graphs, device resident -------------------
+    for _ in range(args.warmup):
+        pair_graph()
+    torch.cuda.synchronize()
+    sampler = clock_sampler_start(_clock_path(rank)) if rank == 0 else None
+    t_graph = max_over_ranks(time_events(pair_graph, args.steps, flush), world, dev)
+
+    def pair_eager():
+        S.forward(x_dev, y_eager)
+        S.adjoint(y_eager, xa_eager)
+
+    for _ in range(2):
+        pair_eager()
+    t_eager = time_events(pair_eager, args.steps, flush) / args.steps
+
+    Kp = int(np.prod(w["Kd"]))
+    grid = torch.empty((F * C * Kp,), dtype=torch.complex64, device=dev)
+
+    def spread():
+        S.plan.interp_adjoint(y_eager, grid, C)
+
+    def gather():
+        S.plan.interp_forward(grid, y_eager, C)
+
+    for _ in range(2):
+        spread()
+        gather()
+    t_spread = time_events(spread, args.steps, flush) / args.steps
+    t_gather = time_events(gather, args.steps, flush) / args.steps
+    clocks = clock_sampler_stop(sampler, _clock_path(rank), dev.index) if rank == 0 else None
+    del grid
+
+    # ---- plain per-call: one single-coil operator per frame ------------------
+    ops = [NufftBase(w["Nd"], oms[f], Jd=w["Jd"], Kd=w["Kd"], Ld=w["L"], on_gpu=True, max_coils=1).plan
+           for f in range(F)]
+    x1 = [[x_dev[f, c:c + 1].contiguous() for c in range(C)] for f in range(F)]
+    y1 = [torch.empty((1, oms[f].shape[0]), dtype=torch.complex64, device=dev) for f in range(F)]
+    xa1 = torch.empty_like(x1[0][0])
+
+    def per_call():
+        for f in range(F):
+            for c in range(C):
+                ops[f].forward(x1[f][c], y1[f], 1)
+                ops[f].adjoint(y1[f], xa1, 1)
+
+    per_call()
+    per_steps = max(2, args.steps // 4)
+    t_percall = time_events(per_call, per_steps, flush) / per_steps
+    del ops, x1, y1
+
+    # ---- end to end: host images in, host samples and images out -----------
+    x_pin = torch.from_numpy(x_host).pin_memory()
+    y_pin = torch.empty((C * S.M_total,), dtype=torch.complex64).pin_memory()
+    xa_pin = torch.empty_like(x_pin).pin_memory()
+
+    def e2e():
+        S.x_static.copy_(x_pin, non_blocking=True)
+        pair_graph()
+        y_pin.copy_(S.y_static, non_blocking=True)
+        xa_pin.copy_(S.xa_static, non_blocking=True)
+        torch.cuda.current_stream().synchronize()
+
+    e2e()
+    e2e_steps = max(3, args.steps // 2)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        e2e()
+    t_e2e = (time.perf_counter() - t0) / e2e_steps
+
+    if rank != 0:
+        return
+    units = F * C
+    ms_per_step = t_graph / args.steps
+    hbm, peak_kind = peaks()
+    M = S.M_total
+    B_alg = C * M * 8 + M * 2 * 4 + F * C * Kp * 8
+    dominant = "spread" if t_spread >= t_gather else "gather"
+    achieved = B_alg / (max(t_spread, t_gather) * 1e-3) / 1e9
+    # CPU baseline: frames 0-3 with one oracle operator per frame
+    cpu_ops = [(_cpu_operator(oms[f], w), np.asfortranarray(np.moveaxis(_series_images_host(w, f), 0, -1)))
+               for f in range(4)]
+    for (op, _), x in cpu_ops:
+        op.adj(op.fft(x))
+    t0 = time.perf_counter()
+    reps = 0
+    while True:
+        for (op, _), x in cpu_ops:
+            op.adj(op.fft(x))
+        reps += 1
+        if time.perf_counter() - t0 > 10.0 or reps >= 20:
+            break
+    cpu_per = (time.perf_counter() - t0) / reps
+    line = {
+        "metric": METRIC, "value": job_value(units, world, ms_per_step), "unit": UNIT,
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "complex64",
+        "data": "synthetic",
+        "config": config_dict({"samples": int(M), "tile": list(tile), "stile": list(stile),
+                               "graph": True}),
+        "eager": {"ms_per_step": t_eager, "value": units / (t_eager * 1e-3)},
+        "per_call": {"value": units / (t_percall * 1e-3), "unit": UNIT, "ms_per_step": t_percall,
+                     "calls_per_step": 2 * units,
+                     "batched_over_per_call": t_percall / ms_per_step},
+        "roofline": {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": hbm,
+                     "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / hbm,
+                     "traffic": None, "algorithmic_bytes": B_alg,
+                     "kernel_ms": {"spread": t_spread, "gather": t_gather}},
+        "cpu_baseline": {"value": 4 * C / cpu_per, "unit": UNIT, "cores": os.cpu_count(),
+                         "kind": cpu_ops[0][0][1],
+                         "sample": "%d x fwd+adj of frames 0-3 (%d coils each), %.2f s each" % (reps, C, cpu_per)},
+        "e2e": {"value": units / t_e2e, "unit": UNIT, "h2d_bytes_per_step": int(x_pin.numel() * 8),
+                "d2h_bytes_per_step": int((y_pin.numel() + xa_pin.numel()) * 8), "seconds_per_step": t_e2e},
+        "gpu_launches": launches_per_step * args.steps,
+        "clocks": clocks,
+        "parity": parity,
+        "autotune": report,
+        "plan": stats,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def run_profile(args):
     """The workload's launches alone, for a profiler to capture."""
     import torch
@@ -380,16 +646,18 @@ def run_profile(args):
     from mrrt.nufft_gb300 import NufftBase
 
     w = WORKLOAD
+    if w["kind"] == "series":
+        raise SystemExit("--profile covers the single-operator workloads")
     C = w["coils"]
     omega, x_f = build_inputs()
     A = NufftBase(Nd=w["Nd"], omega=omega, Jd=w["Jd"], Kd=w["Kd"], Ld=w["L"], precision="single",
                   on_gpu=True, max_coils=C)
     P = A.plan
     dev = torch.device("cuda", torch.cuda.current_device())
-    x_dev = torch.from_numpy(np.ascontiguousarray(np.moveaxis(x_f, -1, 0).transpose(0, 2, 1))).to(dev)
+    x_dev = torch.from_numpy(plan_layout(x_f)).to(dev)
     y_dev = torch.empty((C, A.M), dtype=torch.complex64, device=dev)
     xa_dev = torch.empty_like(x_dev)
-    grid = torch.empty((C, w["Kd"][0] * w["Kd"][1]), dtype=torch.complex64, device=dev)
+    grid = torch.empty((C, int(np.prod(w["Kd"]))), dtype=torch.complex64, device=dev)
     for _ in range(args.warmup + args.steps):
         P.forward(x_dev, y_dev, C)
         P.adjoint(y_dev, xa_dev, C)
@@ -407,7 +675,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--profile", action="store_true", help="launch the workload's kernels only (no timing)")
+    ap.add_argument("--workload", default="2d-multicoil-radial", choices=sorted(WORKLOADS))
     args = ap.parse_args()
+    global WORKLOAD
+    WORKLOAD = WORKLOADS[args.workload]
     if args.profile:
         import torch
 

@@ -142,6 +142,18 @@ int gbn_interp_adjoint(gbn_plan* plan, const void* y, void* grid, int coils,
 int gbn_interp_adjoint_noalloc(gbn_plan* plan, const void* y, void* grid,
                                int coils, void* stream);
 
+/* Sparse-matrix mode: interpolate with precomputed weights instead of the
+ * tables.  w_re[d] (and w_im[d] for phasing complex) are host arrays
+ * [M_total][Jd[d]] in the plan precision: the coefficient of tap j of
+ * sample m on memory axis d, the tap cells being first_tap + j as in table
+ * mode.  The interpolation matrix is their per-sample outer product, as in
+ * the reference's sparse operator (_init_sparsemat,
+ * mrrt/nufft/_nufft.py:750-877, applied as p * xk / p.H * xk at
+ * _nufft.py:1384 and 1505).  w_re NULL returns to table mode;
+ * gbn_plan_set_points drops the weights.                                     */
+int gbn_plan_set_weights(gbn_plan* plan, const void* const* w_re,
+                         const void* const* w_im);
+
 /* Upload derivative tables dh/dt (host, length Jd[d]*L+1 per memory axis, plan
  * precision) used by gbn_grad_tm.  No counterpart in the reference.          */
 int gbn_plan_set_dtables(gbn_plan* plan, const void* const* dtab);

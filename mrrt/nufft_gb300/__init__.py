@@ -11,6 +11,7 @@ from ._dtft import dtft, dtft_adj  # noqa: F401
 from ._kaiser_bessel import kaiser_bessel, kaiser_bessel_ft  # noqa: F401
 from ._kernels import BeattyKernel, KaiserBesselKernel  # noqa: F401
 from ._nufft import NufftBase  # noqa: F401
+from .autograd import NufftOperator, nufft_adjoint, nufft_forward  # noqa: F401
 
 __version__ = "0.1.0"
 
@@ -20,6 +21,9 @@ __all__ = [
     "BeattyKernel",
     "KaiserBesselKernel",
     "NufftBase",
+    "NufftOperator",
+    "nufft_forward",
+    "nufft_adjoint",
     "kaiser_bessel",
     "kaiser_bessel_ft",
 ]

@@ -48,20 +48,87 @@ def _to_numpy(a):
     return np.asarray(a)
 
 
+def deapodisation(Nd, Kd, Jd, n_mid, alpha, rdt):
+    """Scaling factors ``sn`` (mrrt/nufft/_nufft.py:726-748): the float64 outer
+    product of 1 / KB-transform per axis, cast to the operator's real dtype,
+    Fortran order."""
+    sn = np.array([1.0])
+    for d in range(len(Nd)):
+        nc = np.arange(-n_mid[d], -n_mid[d] + Nd[d])
+        tmp = 1 / kaiser_bessel_ft(nc / Kd[d], Jd[d], alpha[d], 0, 1)
+        sn = np.outer(sn.ravel(), tmp.conj())
+    return np.asfortranarray(sn.reshape(tuple(Nd)).astype(rdt))
+
+
+def sample_phase_of(omega, n_shift, n_mid, phasing, rdt, cdt):
+    """Per-sample phase (mrrt/nufft/_nufft.py:717-724, 898-903): phase_after =
+    exp(i omega . (n_shift - n_mid)) for real phasing (omega in its given
+    dtype, the shift vector in the operator's real dtype); for complex phasing
+    exp(i omega . n_shift) when the shift is non-zero, else None."""
+    if phasing == "real":
+        shift_vec = [(s - m) for s, m in zip(n_shift, n_mid)]
+        return np.exp(1j * np.dot(omega, np.asarray(shift_vec, dtype=rdt))).astype(cdt, copy=False)
+    if any(s != 0 for s in n_shift):
+        return np.exp(1j * np.dot(omega.astype(rdt), np.asarray(n_shift))).astype(cdt)
+    return None
+
+
+def normalised_coordinates(omega, Kd, rdt):
+    """tm = omega / (2 pi / K_d) in the operator's real dtype
+    (mrrt/nufft/_nufft.py:1012-1016)."""
+    omega = np.asarray(omega, dtype=rdt)
+    tm = np.zeros_like(omega)
+    for d in range(omega.shape[1]):
+        gam = 2 * np.pi / Kd[d]
+        tm[:, d] = omega[:, d] / gam
+    return tm
+
+
+def sparse_weights(omega, Nd, Jd, Kd, kernel, phasing, rdt):
+    """Per-axis factors of the reference's sparse interpolation matrix
+    (``_init_sparsemat``, mrrt/nufft/_nufft.py:750-877, with ``_nufft_offset``
+    and ``_nufft_coef``, mrrt/nufft/_utils.py:20-86): for sample m and tap j
+    of axis d, ``u = kernel_d(dk_m - (j + 1))`` with
+    ``dk = om / gam - floor(om / gam - J / 2)`` (om in the operator's real
+    dtype), times ``exp(i gam (N - 1) / 2 * arg)`` for complex phasing.  The
+    matrix entry is the conjugate of the product over axes, so the factors
+    are returned conjugated.  Returns ``(w_re, w_im)``: lists of
+    ``[M, J_d]`` arrays (``w_im`` None for real phasing)."""
+    w_re, w_im = [], []
+    for d in range(len(Nd)):
+        J, K, N = Jd[d], Kd[d], Nd[d]
+        om = omega[:, d]
+        gam = 2 * np.pi / K
+        koff = np.floor(om / gam - J / 2.0)
+        dk = om / gam - koff
+        arg = -np.arange(1, J + 1)[:, None] + dk[None, :]      # [J, M]
+        c = kernel.kernels[d](arg)
+        if phasing == "complex":
+            u = np.conj(np.exp(1j * gam * (N - 1) / 2.0 * arg) * c)
+            w_re.append(np.ascontiguousarray(u.real.T, dtype=rdt))
+            w_im.append(np.ascontiguousarray(u.imag.T, dtype=rdt))
+        else:
+            w_re.append(np.ascontiguousarray(np.asarray(c).real.T, dtype=rdt))
+    return w_re, (w_im if phasing == "complex" else None)
+
+
 class NufftBase(object):
     """Non-uniform FFT operator (table-based interpolation) on the GPU.
 
     Parameters are those of the reference ``NufftBase``; see the module
     docstring for the data conventions.  ``mode`` must be ``'table'``.
 
-    Extra keyword (not in the reference): ``max_coils`` -- the repetition
+    Extra keywords (not in the reference): ``max_coils`` -- the repetition
     count the tile plan is sized for (default 1).  Any batch size works; a
     batch wider than the tiles were sized for runs in more coil chunks.
+    ``tile`` / ``stile`` -- gather / spread tile edges per axis (default: the
+    planner's choice; ``autotune.tune_operator`` measures the best).
     """
 
     def __init__(self, Nd, omega, Jd=4, Kd=None, precision="single", mode="table", Ld=1024,
                  ortho=False, n_shift=None, phasing="real", adjoint_scalefactor=1.0,
-                 preplan_cufft=True, order="F", verbose=False, on_gpu=False, max_coils=1):
+                 preplan_cufft=True, order="F", verbose=False, on_gpu=False, max_coils=1,
+                 tile=None, stile=None):
         require_cuda()
         self.verbose = verbose
         self.order = order
@@ -83,15 +150,12 @@ class NufftBase(object):
         self.__Kd = _as_tuple(Kd, type=int, n=self.ndim)
         self.ortho = ortho
         self.scale_ortho = math.sqrt(math.prod(self.__Kd)) if ortho else 1
-        if mode != "table":
-            if mode == "sparse":
-                raise NotImplementedError(
-                    "mode='sparse' is not provided by the GPU operator; use mode='table'")
+        if mode not in ("table", "sparse"):
             raise ValueError("Invalid NUFFT mode: {}".format(mode))
         self.__mode = mode
         self.adjoint_scalefactor = adjoint_scalefactor
         self.preplan_cufft = preplan_cufft
-        self.p = None
+        self._p = None
         self.__Ld = int(Ld)
         if self.__Ld % 2 == 1 and any(j % 2 == 1 for j in self.__Jd):
             warnings.warn("accuracy may be compromised when L and J are both odd")
@@ -125,34 +189,18 @@ class NufftBase(object):
 
         self.kernel = BeattyKernel(shape=self.__Jd, grid_shape=self.__Nd, os_grid_shape=self.__Kd)
         rdt, cdt = self._real_dtype, self._cplx_dtype
-        # deapodisation: float64 outer product, then the operator dtype
-        sn = np.array([1.0])
-        for d in range(self.ndim):
-            nc = np.arange(-self.n_mid[d], -self.n_mid[d] + self.__Nd[d])
-            tmp = 1 / kaiser_bessel_ft(nc / self.__Kd[d], self.__Jd[d], self.kernel.alpha[d], 0, 1)
-            sn = np.outer(sn.ravel(), tmp.conj())
-        self.sn = np.asfortranarray(sn.reshape(self.__Nd).astype(rdt))
-        # per-sample phase (mrrt/nufft/_nufft.py:717-724, 898-903): omega in its
-        # given dtype, the shift vector in the operator's real dtype
+        self.sn = deapodisation(self.__Nd, self.__Kd, self.__Jd, self.n_mid, self.kernel.alpha, rdt)
         if phasing == "real":
-            shift_vec = [(s - m) for s, m in zip(self.__n_shift, self.n_mid)]
-            self.phase_after = np.exp(1j * np.dot(omega, np.asarray(shift_vec, dtype=rdt))).astype(cdt, copy=False)
+            self.phase_after = sample_phase_of(omega, self.__n_shift, self.n_mid, "real", rdt, cdt)
             self.phase_shift = None
             sample_phase = self.phase_after
         else:
             self.phase_after = None
-            if any(s != 0 for s in self.__n_shift):
-                self.phase_shift = np.exp(1j * np.dot(omega.astype(rdt), np.asarray(self.__n_shift))).astype(cdt)
-            else:
-                self.phase_shift = None
+            self.phase_shift = sample_phase_of(omega, self.__n_shift, self.n_mid, "complex", rdt, cdt)
             sample_phase = self.phase_shift
         self.__omega = np.asfortranarray(omega.astype(rdt))
         self.M = self.__omega.shape[0]
-        tm = np.zeros_like(self.__omega)
-        for d in range(self.ndim):
-            gam = 2 * np.pi / self.__Kd[d]
-            tm[:, d] = self.__omega[:, d] / gam
-        self.tm = tm
+        self.tm = normalised_coordinates(self.__omega, self.__Kd, rdt)
         tdt = cdt if phasing == "complex" else rdt
         self.h = [kernel_table(self.__Nd[d], self.__Jd[d], self.__Kd[d], self.__Ld, phasing, tdt)
                   for d in range(self.ndim)]
@@ -165,9 +213,15 @@ class NufftBase(object):
             self.__Nd, self.__Kd, self.__Jd, self.__Ld, rdt,
             [np.real(h) for h in self.h],
             [np.imag(h) for h in self.h] if phasing == "complex" else None,
-            self.sn.ravel(order="F"), np.ascontiguousarray(tm), sample_phase,
+            self.sn.ravel(order="F"), np.ascontiguousarray(self.tm), sample_phase,
             ortho=ortho, adjoint_scale=adjoint_scalefactor, pb_coef=pb_coef,
-            pb_order=list(range(self.ndim)), phasing=phasing, max_coils=max_coils)
+            pb_order=list(range(self.ndim)), phasing=phasing, max_coils=max_coils,
+            tile=tile, stile=stile)
+        self._p = None
+        if mode == "sparse":
+            self._weights = sparse_weights(self.__omega, self.__Nd, self.__Jd, self.__Kd, self.kernel,
+                                           phasing, rdt)
+            self._plan.set_weights(*self._weights)
 
     # ------------------------------------------------------------------ props
     @property
@@ -214,6 +268,41 @@ class NufftBase(object):
     def plan(self):
         """The underlying :class:`GpuPlan` (memory-axis order = reference axis order)."""
         return self._plan
+
+    @property
+    def p(self):
+        """Sparse mode: the interpolation matrix [M, prod(Kd)] as a scipy CSC
+        matrix on the host (the reference's ``self.p``), built on first
+        access from the uploaded weights; None in table mode.  The GPU path
+        never uses it."""
+        if self.__mode != "sparse":
+            return None
+        if self._p is None:
+            import scipy.sparse
+
+            w_re, w_im = self._weights
+            M = self.M
+            rows = np.arange(M)
+            kk = np.zeros((M, 1), dtype=np.int64)
+            uu = np.ones((M, 1), dtype=self._cplx_dtype if w_im is not None else self._real_dtype)
+            stride = 1
+            for d in range(self.ndim):
+                J, K = self.__Jd[d], self.__Kd[d]
+                gam = 2 * np.pi / K
+                koff = np.floor(self.__omega[:, d] / gam - J / 2.0).astype(np.int64)
+                kd = np.mod(koff[:, None] + np.arange(1, J + 1)[None, :], K) * stride
+                wd = w_re[d] if w_im is None else w_re[d] + 1j * w_im[d]
+                kk = (kk[:, :, None] + kd[:, None, :]).reshape(M, -1, order="F")
+                uu = (uu[:, :, None] * wd[:, None, :]).reshape(M, -1, order="F")
+                stride *= K
+            if self.__phasing == "complex" and self.phase_shift is not None:
+                # the reference folds the n_shift phase into the rows
+                # (_nufft.py:836-844); the GPU applies it as the sample phase
+                uu = uu * self.phase_shift[:, None]
+            mm = np.repeat(rows[:, None], kk.shape[1], axis=1)
+            self._p = scipy.sparse.coo_matrix((uu.ravel(), (mm.ravel(), kk.ravel())),
+                                              shape=(M, int(np.prod(self.__Kd)))).tocsc()
+        return self._p
 
     @property
     def phase_before(self):

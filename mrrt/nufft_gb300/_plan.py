@@ -168,6 +168,20 @@ class GpuPlan:
                                             ctypes.c_void_p(gtm.data_ptr()), int(coils), _stream()))
         return gtm
 
+    def set_weights(self, w_re, w_im=None):
+        """Sparse-matrix mode: per-axis weights [M_total, J_d] (plan precision)
+        replace the table interpolation; ``None`` returns to table mode."""
+        if w_re is None:
+            with torch.cuda.device(self.device):
+                _lib.check(self.lib.gbn_plan_set_weights(self.handle, None, None))
+            return
+        wr = [np.ascontiguousarray(w, dtype=self.rdt) for w in w_re]
+        wi = [np.ascontiguousarray(w, dtype=self.rdt) for w in w_im] if w_im is not None else None
+        Wr = (ctypes.c_void_p * 3)(*[_vp(w) for w in wr] + [None] * (3 - len(wr)))
+        Wi = (ctypes.c_void_p * 3)(*[_vp(w) for w in wi] + [None] * (3 - len(wi))) if wi else None
+        with torch.cuda.device(self.device):
+            _lib.check(self.lib.gbn_plan_set_weights(self.handle, Wr, Wi))
+
     def set_points(self, tm, sample_phase):
         tm = np.ascontiguousarray(tm, dtype=self.rdt).reshape(-1, self.ndim)
         if tm.shape[0] != self.M_total:

@@ -89,6 +89,21 @@ __device__ __forceinline__ void table_coef(const Geom<R>& g, int d, R t, int k, 
     }
 }
 
+// Coefficient of tap j (0 <= j < J) of sample `gs` (index in sample order)
+// on axis d: the precomputed weight in sparse-matrix mode, else the table
+// interpolation at t for tap k = first tap + j.
+template <typename R, bool CX>
+__device__ __forceinline__ void tap_coef(const Geom<R>& g, int d, R t, int kf, int j, int64_t gs, R& cr,
+                                         R& ci) {
+    if (g.wr[0]) {
+        const int64_t w = gs * g.J[d] + j;
+        cr = __ldg(g.wr[d] + w);
+        ci = CX ? __ldg(g.wi[d] + w) : (R)0;
+    } else {
+        table_coef<R, CX>(g, d, t, kf + j, cr, ci);
+    }
+}
+
 // Tile coordinates of a linear tile index (axis 0 fastest).
 template <int NDIM>
 __device__ __forceinline__ void tile_origin(int tile, const int* nt, const int* T, int* org) {

@@ -119,6 +119,8 @@ gather_kernel(const GatherParams<R> p) {
             for (int j = 0; j < JL; ++j) mcr[d][j] = mci[d][j] = (R)0;
         if (lane < nb) {
             const int e = start + base + lane;
+            midx = p.s.idx[e];
+            const int64_t gs = fo + midx;
             int loc[3] = {0, 0, 0};
 #pragma unroll
             for (int d = 0; d < NDIM; ++d) {
@@ -127,10 +129,9 @@ gather_kernel(const GatherParams<R> p) {
                 loc[d] = wrapk(kf, g.K[d]) - org[d];
 #pragma unroll
                 for (int j = 0; j < JL; ++j)
-                    if (JJ > 0 || j < g.J[d]) table_coef<R, CX>(g, d, t, kf + j, mcr[d][j], mci[d][j]);
+                    if (JJ > 0 || j < g.J[d]) tap_coef<R, CX>(g, d, t, kf, j, gs, mcr[d][j], mci[d][j]);
             }
             mbase = ((loc[2] * Rd[1] + loc[1]) * Rd[0] + loc[0]) * LSP;
-            midx = p.s.idx[e];
             if (p.apply_ph) mph = p.s.ph[e];
         }
         for (int s0 = 0; s0 < nb; s0 += SW) {
@@ -216,8 +217,7 @@ size_t gather_smem(const Geom<R>& g, const Lanes& ln) {
 
 template <typename K>
 static cudaError_t ensure_smem(K kernel, size_t bytes) {
-    if (bytes <= 48 * 1024) return cudaSuccess;
-    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    return ensure_dynamic_smem(reinterpret_cast<const void*>(kernel), bytes);
 }
 
 template <typename R, int NDIM, bool CX, int JJ, int LSC>

@@ -34,6 +34,11 @@ struct Geom {
     int ncenter[3];          // floor(J*L/2): table index of t = 0
     const R* hr[3];          // device tables (shifted past their zero padding)
     const R* hi[3];          // imaginary tables, nullptr for a real kernel
+    // Precomputed interpolation weights (sparse-matrix mode): per axis
+    // [M_total][J] in sample order (frame offset + index), used instead of
+    // the tables when wr[0] is set; wi imaginary parts or nullptr.
+    const R* wr[3];
+    const R* wi[3];
     int64_t Kprod, Nprod;
     R pbc[3];                // phase_before coefficient per memory axis
     int pbo[3];              // summation order of the per-axis phases
@@ -154,6 +159,12 @@ template <typename R> size_t gather_smem(const Geom<R>& g, const Lanes& ln);
 template <typename R> size_t spread_smem(const Geom<R>& g, const Lanes& ln);
 // Threads of a spread CTA for a tiling (one warp per register block).
 int spread_threads(int ndim, const int* T);
+
+// Raise a kernel's dynamic shared-memory limit to at least `bytes` on the
+// current device.  The attribute is set once per (kernel, device) and size
+// (later launches needing no more skip the call), so launches recorded in a
+// CUDA graph after a warm-up call make no attribute call.
+cudaError_t ensure_dynamic_smem(const void* kernel, size_t bytes);
 
 // Address and size of the fixed no-alloc scratch array on the current device
 // (gbn_noalloc.cu); looked up on the first request per device.

@@ -22,6 +22,32 @@
 
 using namespace gbn;
 
+namespace gbn {
+
+cudaError_t ensure_dynamic_smem(const void* kernel, size_t bytes) {
+    if (bytes <= 48 * 1024) return cudaSuccess;
+    struct Entry { const void* k; int dev; size_t bytes; };
+    static std::mutex mu;
+    static std::vector<Entry> done;
+    int dev = -1;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lk(mu);
+    for (auto& x : done)
+        if (x.k == kernel && x.dev == dev && x.bytes >= bytes) return cudaSuccess;
+    e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e != cudaSuccess) return e;
+    for (auto& x : done)
+        if (x.k == kernel && x.dev == dev) {
+            x.bytes = bytes;
+            return cudaSuccess;
+        }
+    done.push_back({kernel, dev, bytes});
+    return cudaSuccess;
+}
+
+}  // namespace gbn
+
 namespace {
 
 thread_local std::string g_last_error;
@@ -117,6 +143,7 @@ struct gbn_plan {
     bool has_phase = false;
 
     DevBuf tables, dtables, sn, dfoff;
+    DevBuf weights;       // sparse-matrix mode: per-axis [M_total][J] weights (re, then im)
     DevBuf glist, gitems;
     DevBuf slist, sitems, sparts, rtiles;
     int n_gitems = 0, n_sitems = 0, n_rtiles = 0, n_slots = 0;
@@ -175,6 +202,18 @@ Geom<R> make_geom(const gbn_plan* P, bool spread) {
         const size_t len = (size_t)G.Jd[d] * G.L + 1 + 4;
         g.hi[d] = base + off + 2;
         off += len;
+    }
+    if (P->weights.p) {
+        const R* w = reinterpret_cast<const R*>(P->weights.p);
+        size_t woff = 0;
+        for (int d = 0; d < G.ndim; ++d) {
+            g.wr[d] = w + woff;
+            woff += (size_t)P->M_total * G.Jd[d];
+        }
+        for (int d = 0; d < G.ndim && P->cx; ++d) {
+            g.wi[d] = w + woff;
+            woff += (size_t)P->M_total * G.Jd[d];
+        }
     }
     g.L = G.L;
     g.Kprod = P->Kprod;
@@ -890,6 +929,8 @@ int gbn_plan_set_points(gbn_plan* P, const void* tm, const void* sample_phase) {
     std::lock_guard<std::mutex> lk(P->mu);
     DeviceGuard guard(P->device);
     GBN_CUDA(cudaDeviceSynchronize(), "synchronise before replanning");
+    // weights belong to the old coordinates
+    GBN_CUDA(P->weights.alloc(0), "weight release");
     return P->dbl ? plan_points<double>(P, tm, sample_phase) : plan_points<float>(P, tm, sample_phase);
 }
 
@@ -986,6 +1027,36 @@ int gbn_plan_set_dtables(gbn_plan* P, const void* const* dtab) {
     return GBN_OK;
 }
 
+int gbn_plan_set_weights(gbn_plan* P, const void* const* w_re, const void* const* w_im) {
+    if (!P) return fail(GBN_ERR_INVALID, "null plan");
+    std::lock_guard<std::mutex> lk(P->mu);
+    DeviceGuard guard(P->device);
+    GBN_CUDA(cudaDeviceSynchronize(), "synchronise before replacing weights");
+    if (!w_re) {
+        GBN_CUDA(P->weights.alloc(0), "weight release");
+        return GBN_OK;
+    }
+    const gbn_geometry& G = P->geom;
+    if (P->cx && !w_im) return fail(GBN_ERR_INVALID, "complex phasing needs imaginary weights");
+    size_t per = 0;
+    for (int d = 0; d < G.ndim; ++d) {
+        if (!w_re[d] || (P->cx && !w_im[d])) return fail(GBN_ERR_INVALID, "missing weight array");
+        per += (size_t)P->M_total * G.Jd[d];
+    }
+    const size_t bytes = per * (P->cx ? 2 : 1) * P->rsize;
+    if (bytes == 0) return GBN_OK;
+    GBN_CUDA(P->weights.alloc(bytes), "weight allocation");
+    size_t off = 0;
+    for (int part = 0; part < (P->cx ? 2 : 1); ++part)
+        for (int d = 0; d < G.ndim; ++d) {
+            const size_t n = (size_t)P->M_total * G.Jd[d] * P->rsize;
+            const void* src = part == 0 ? w_re[d] : w_im[d];
+            GBN_CUDA(cudaMemcpy(static_cast<char*>(P->weights.p) + off, src, n, cudaMemcpyHostToDevice),
+                     "weight upload");
+            off += n;
+        }
+    return GBN_OK;
+}
 
 int gbn_grad_tm(gbn_plan* P, const void* grid, const void* gy, const double* phase_shift, void* gtm,
                 int coils, void* stream) {
@@ -995,6 +1066,7 @@ int gbn_grad_tm(gbn_plan* P, const void* grid, const void* gy, const double* pha
     if (P->F != 1) return fail(GBN_ERR_UNSUPPORTED, "coordinate gradient needs a single-frame plan");
     if (P->cx) return fail(GBN_ERR_UNSUPPORTED, "coordinate gradient needs phasing real");
     if (!P->dtables.p) return fail(GBN_ERR_INVALID, "derivative tables not set (gbn_plan_set_dtables)");
+    if (P->weights.p) return fail(GBN_ERR_UNSUPPORTED, "coordinate gradient needs table interpolation");
     std::lock_guard<std::mutex> lk(P->mu);
     DeviceGuard guard(P->device);
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
@@ -1032,7 +1104,7 @@ int gbn_plan_stats(const gbn_plan* P, int64_t* o) {
     o[3] = P->glen;
     o[4] = P->slen;
     o[5] = (int64_t)P->ntiles_s * P->F;
-    o[6] = (int64_t)(P->tables.bytes + P->sn.bytes + P->glist.bytes + P->slist.bytes + P->pad.bytes +
+    o[6] = (int64_t)(P->tables.bytes + P->weights.bytes + P->sn.bytes + P->glist.bytes + P->slist.bytes + P->pad.bytes +
                      P->grid.bytes + P->scratch.bytes);
     o[7] = P->M_total;
     return GBN_OK;

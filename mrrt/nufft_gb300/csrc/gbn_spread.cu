@@ -205,7 +205,8 @@ spread_kernel(const SpreadParams<R> p) {
             }
             const R t = tb[(b * NDIM + d) * CH + el];
             R cr, ci;
-            table_coef<R, CX>(g, d, t, first_tap(t, Jd) + j, cr, ci);
+            const int64_t gs = g.wr[0] ? fo + p.s.idx[start + k * CH + el] : 0;
+            tap_coef<R, CX>(g, d, t, first_tap(t, Jd), j, gs, cr, ci);
             cp[el * SL::PSTR + slot0 + j] = CX ? cmake<R>(cr, -ci) : cmake<R>(cr, cr);
         }
         // ---- copy-in of chunk k+1 overlaps with the accumulation of chunk k ----
@@ -356,12 +357,18 @@ spread_kernel(const SpreadParams<R> p) {
     }
 }
 
-// Sum the parts of split tiles in part order and write the grid.
+// Sum the parts of split tiles in part order and write the grid.  One
+// thread per (coil, cell) of a tile; a tile's TT x LS elements are spread
+// over `nsub` CTAs (blockIdx.x = tile * nsub + sub) so that the many small
+// partial-sum reads are in flight at once.  The parts are loaded four at a
+// time and added in part order, so the result is the same in every run.
 template <typename R, int NDIM>
-__global__ void __launch_bounds__(256) reduce_kernel(const ReduceParams<R> p) {
+__global__ void __launch_bounds__(256) reduce_kernel(const ReduceParams<R> p, const int nsub) {
     typedef typename Cx<R>::T C;
     const Geom<R>& g = p.g;
-    const int4 tl = p.tiles[blockIdx.x];
+    const int ti = blockIdx.x / nsub;
+    const int sub = blockIdx.x - ti * nsub;
+    const int4 tl = p.tiles[ti];
     const int f = tl.x, tile = tl.y, slot0 = tl.z, nparts = tl.w;
     const int LS = p.ln.LS, lsh = p.ln.lsh;
     const int c0 = blockIdx.y << lsh;
@@ -374,34 +381,47 @@ __global__ void __launch_bounds__(256) reduce_kernel(const ReduceParams<R> p) {
         ext[d] = min(g.T[d], g.K[d] - org[d]);
     }
     const int TT = Td[0] * Td[1] * Td[2];
-    for (int q = threadIdx.x; q < TT * nc; q += blockDim.x) {
-        const int c = q / TT;
-        const int cell = q - c * TT;
-        int r[3];
-        r[0] = cell % Td[0];
-        r[1] = (cell / Td[0]) % Td[1];
-        r[2] = cell / (Td[0] * Td[1]);
-        bool inside = true;
+    const int q = sub * blockDim.x + threadIdx.x;
+    if (q >= TT * nc) return;
+    const int c = q / TT;
+    const int cell = q - c * TT;
+    int r[3];
+    r[0] = cell % Td[0];
+    r[1] = (cell / Td[0]) % Td[1];
+    r[2] = cell / (Td[0] * Td[1]);
+    bool inside = true;
 #pragma unroll
-        for (int d = 0; d < NDIM; ++d) inside = inside && (r[d] < ext[d]);
-        if (!inside) continue;
-        C acc = cmake<R>((R)0, (R)0);
-        for (int s = 0; s < nparts; ++s) {
-            const C v = p.scratch[(((int64_t)(slot0 + s) * gridDim.y + blockIdx.y) * LS + c) * p.tile_cells + cell];
-            acc.x += v.x;
-            acc.y += v.y;
-        }
-        int k[3] = {0, 0, 0};
-        int64_t off = 0, stride = 1;
-#pragma unroll
-        for (int d = 0; d < NDIM; ++d) {
-            k[d] = org[d] + r[d];
-            off += (int64_t)k[d] * stride;
-            stride *= g.K[d];
-        }
-        if (p.apply_pb) acc = cmulc(acc, phase_before(g, k));
-        p.grid[((int64_t)f * p.coils + c0 + c) * g.Kprod + off] = acc;
+    for (int d = 0; d < NDIM; ++d) inside = inside && (r[d] < ext[d]);
+    if (!inside) return;
+    const int64_t pstride = (int64_t)gridDim.y * LS * p.tile_cells;
+    const C* src = p.scratch + (((int64_t)slot0 * gridDim.y + blockIdx.y) * LS + c) * p.tile_cells + cell;
+    C acc = cmake<R>((R)0, (R)0);
+    int s = 0;
+    for (; s + 4 <= nparts; s += 4) {
+        const C v0 = src[(int64_t)s * pstride];
+        const C v1 = src[(int64_t)(s + 1) * pstride];
+        const C v2 = src[(int64_t)(s + 2) * pstride];
+        const C v3 = src[(int64_t)(s + 3) * pstride];
+        acc.x += v0.x; acc.y += v0.y;
+        acc.x += v1.x; acc.y += v1.y;
+        acc.x += v2.x; acc.y += v2.y;
+        acc.x += v3.x; acc.y += v3.y;
     }
+    for (; s < nparts; ++s) {
+        const C v = src[(int64_t)s * pstride];
+        acc.x += v.x;
+        acc.y += v.y;
+    }
+    int k[3] = {0, 0, 0};
+    int64_t off = 0, stride = 1;
+#pragma unroll
+    for (int d = 0; d < NDIM; ++d) {
+        k[d] = org[d] + r[d];
+        off += (int64_t)k[d] * stride;
+        stride *= g.K[d];
+    }
+    if (p.apply_pb) acc = cmulc(acc, phase_before(g, k));
+    p.grid[((int64_t)f * p.coils + c0 + c) * g.Kprod + off] = acc;
 }
 
 template <typename R>
@@ -418,8 +438,7 @@ size_t spread_smem(const Geom<R>& g, const Lanes& ln) {
 
 template <typename K>
 static cudaError_t ensure_smem(K kernel, size_t bytes) {
-    if (bytes <= 48 * 1024) return cudaSuccess;
-    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    return ensure_dynamic_smem(reinterpret_cast<const void*>(kernel), bytes);
 }
 
 template <typename R, int NDIM, bool CX, int JJ, int LSC>
@@ -486,11 +505,13 @@ cudaError_t launch_spread(const SpreadParams<R>& p, cudaStream_t s) {
 template <typename R>
 cudaError_t launch_reduce(const ReduceParams<R>& p, cudaStream_t s) {
     if (p.ntiles == 0 || p.coils == 0) return cudaSuccess;
-    dim3 grid(p.ntiles, (p.coils + p.ln.LS - 1) / p.ln.LS);
+    const int64_t tt = (int64_t)p.g.T[0] * (p.g.ndim > 1 ? p.g.T[1] : 1) * (p.g.ndim > 2 ? p.g.T[2] : 1);
+    const int nsub = (int)((tt * p.ln.LS + 255) / 256);
+    dim3 grid((unsigned)((int64_t)p.ntiles * nsub), (p.coils + p.ln.LS - 1) / p.ln.LS);
     switch (p.g.ndim) {
-        case 1: reduce_kernel<R, 1><<<grid, 256, 0, s>>>(p); break;
-        case 2: reduce_kernel<R, 2><<<grid, 256, 0, s>>>(p); break;
-        case 3: reduce_kernel<R, 3><<<grid, 256, 0, s>>>(p); break;
+        case 1: reduce_kernel<R, 1><<<grid, 256, 0, s>>>(p, nsub); break;
+        case 2: reduce_kernel<R, 2><<<grid, 256, 0, s>>>(p, nsub); break;
+        case 3: reduce_kernel<R, 3><<<grid, 256, 0, s>>>(p, nsub); break;
         default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();

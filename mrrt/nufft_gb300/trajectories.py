@@ -90,17 +90,18 @@ def complex_image(shape, seed=0, dtype=np.complex64):
 
 
 def gaussian_coil_maps(Nd, n_coils, sigma_frac=0.3, radius_frac=0.35):
-    """Smooth synthetic 2-D coil maps: Gaussian blobs on a circle, each with
-    phase exp(i 2 pi c / C).  Returns [C, N0, N1]."""
-    N0, N1 = Nd
-    n0 = np.arange(N0)[:, None] - N0 / 2
-    n1 = np.arange(N1)[None, :] - N1 / 2
-    sig = sigma_frac * max(N0, N1)
+    """Smooth synthetic coil maps: Gaussian blobs of width sigma_frac * max(Nd)
+    centred on a circle of radius radius_frac * N in the first two axes (the
+    third axis, if any, is centred), each with phase exp(i 2 pi c / C).
+    Returns [C, *Nd]."""
+    Nd = tuple(Nd)
+    axes = np.meshgrid(*[np.arange(n) - n / 2 for n in Nd], indexing="ij")
+    sig = sigma_frac * max(Nd)
     maps = []
     for c in range(n_coils):
         ang = 2 * np.pi * c / n_coils
-        c0 = radius_frac * N0 * math.cos(ang)
-        c1 = radius_frac * N1 * math.sin(ang)
-        blob = np.exp(-((n0 - c0) ** 2 + (n1 - c1) ** 2) / (2 * sig * sig))
-        maps.append(blob * np.exp(1j * ang))
+        centre = [radius_frac * Nd[0] * math.cos(ang), radius_frac * Nd[1] * math.sin(ang)]
+        centre += [0.0] * (len(Nd) - 2)
+        r2 = sum((a - c0) ** 2 for a, c0 in zip(axes, centre))
+        maps.append(np.exp(-r2 / (2 * sig * sig)) * np.exp(1j * ang))
     return np.stack(maps, axis=0)

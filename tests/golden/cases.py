@@ -78,3 +78,15 @@ def dtft_case():
     x = rs.standard_normal(Nd) + 1j * rs.standard_normal(Nd)
     y = rs.standard_normal(300) + 1j * rs.standard_normal(300)
     return dict(Nd=Nd, omega=omega, x=x, y=y, n_shift=(1.0, 3.0, 2.0))
+
+
+def sparse_cases():
+    """The reference test-suite geometries in sparse-matrix mode
+    (mrrt/nufft/tests/test_nufft.py:99-324 run both modes)."""
+    out = []
+    for name, c in small_cases():
+        kw = dict(c["kw"])
+        kw["mode"] = "sparse"
+        out.append(("sparse_" + name, dict(kw=kw, x=c["x"])))
+    return out
+

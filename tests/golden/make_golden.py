@@ -63,6 +63,8 @@ def main():
             tabs["h_%d_%s" % (n, phasing)] = np.asarray(h)
     np.savez_compressed(os.path.join(HERE, "tables.npz"), **tabs)
 
+    make_sparse(ref)
+
     # 4. exact NUDFT reference values
     d = {}
     c = cases.dtft_case()
@@ -74,5 +76,28 @@ def main():
             print(f, os.path.getsize(os.path.join(HERE, f)))
 
 
+def make_sparse(ref=None):
+    """Sparse-matrix mode on the reference test geometries: forward and
+    adjoint outputs, and the interpolation matrix itself (CSC arrays) for the
+    2-D cases."""
+    ref = ref or load_reference()
+    sp = {}
+    for name, c in cases.sparse_cases():
+        A = ref.NufftBase(**c["kw"])
+        y = A.fft(c["x"])
+        sp[name + "_y"] = y
+        sp[name + "_xadj"] = A.adj(y)
+        if name.startswith("sparse_2d"):
+            p = A.p.tocsc()
+            p.sort_indices()
+            sp[name + "_p_data"] = p.data
+            sp[name + "_p_indices"] = p.indices
+            sp[name + "_p_indptr"] = p.indptr
+    np.savez_compressed(os.path.join(HERE, "sparse_cases.npz"), **sp)
+
+
 if __name__ == "__main__":
-    main()
+    if sys.argv[1:] == ["--sparse-only"]:
+        make_sparse()
+    else:
+        main()

@@ -80,6 +80,24 @@ def test_reference_test_geometries(nb, name):
     np.testing.assert_allclose(y, yt, rtol=rtol, atol=atol)
 
 
+@pytest.mark.parametrize("name", [n for n, _ in cases.sparse_cases()])
+def test_sparse_mode_matches_reference_sparse_operator(nb, name):
+    """mode='sparse' (precomputed kernel weights in place of the table)
+    against the reference's own sparse-matrix operator on its test
+    geometries, both phasings and precisions."""
+    g = cases.load("sparse_cases")
+    c = dict(cases.sparse_cases())[name]
+    A = nb(**c["kw"])
+    tol = tol_for(c["kw"]["precision"])
+    y = A.fft(c["x"])
+    assert rel_l2(y, g[name + "_y"]) < tol
+    assert rel_l2(A.adj(y), g[name + "_xadj"]) < tol
+    kw = c["kw"]
+    yt = O.dtft(c["x"], kw["omega"], kw["Nd"], kw["n_shift"])
+    rtol, atol = (1e-2, 1e-4) if len(kw["Nd"]) == 3 else (1e-3, 1e-5)
+    np.testing.assert_allclose(y, yt, rtol=rtol, atol=atol)
+
+
 @pytest.mark.parametrize("name", [n for n, _ in cases.adj_shift_cases()])
 def test_fractional_shift_adjoint(nb, name):
     g = cases.load("small_cases")

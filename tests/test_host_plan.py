@@ -1,0 +1,72 @@
+"""Host-side plan math of the drop-in ``NufftBase`` on CPU (no GPU): the
+device plan is replaced by a recorder, so these tests check what would be
+uploaded -- deapodisation, tables, coordinates, phases and the sparse-mode
+interpolation weights -- against values the reference itself computed
+(tests/golden)."""
+import numpy as np
+import pytest
+
+from tests.conftest import rel_l2
+from tests.golden import cases
+
+
+class _RecordingPlan:
+    """Stands in for GpuPlan: records the upload, computes nothing."""
+
+    def __init__(self, Nd, Kd, Jd, L, rdt, tables_re, tables_im, sn, tm, sample_phase, **kw):
+        self.args = dict(Nd=Nd, Kd=Kd, Jd=Jd, L=L, rdt=rdt, tables_re=tables_re, tables_im=tables_im,
+                         sn=sn, tm=tm, sample_phase=sample_phase, **kw)
+        self.weights = None
+
+    def set_weights(self, w_re, w_im=None):
+        self.weights = (w_re, w_im)
+
+
+@pytest.fixture
+def host_nufft(monkeypatch):
+    from mrrt.nufft_gb300 import _nufft
+
+    monkeypatch.setattr(_nufft, "require_cuda", lambda: None)
+    monkeypatch.setattr(_nufft, "GpuPlan", _RecordingPlan)
+    return _nufft.NufftBase
+
+
+def test_table_plan_matches_reference_sn_and_table(host_nufft):
+    c = cases.radial_2d_128()
+    g = cases.load("radial128")
+    A = host_nufft(**c["kw"])
+    assert A.sn.dtype == np.float32
+    assert rel_l2(A.sn, g["radial128_sn"]) < 1e-6
+    assert rel_l2(np.asarray(A.h[0]), g["radial128_h0"]) < 1e-6
+    up = A.plan.args
+    assert up["tm"].shape == (A.M, 2) and up["tm"].flags["C_CONTIGUOUS"]
+    np.testing.assert_array_equal(up["tm"], A.tm)
+    assert up["sample_phase"].dtype == np.complex64
+
+
+@pytest.mark.parametrize("name", [n for n, _ in cases.sparse_cases() if n.startswith("sparse_2d")])
+def test_sparse_weights_rebuild_reference_matrix(host_nufft, name):
+    """The per-axis weights uploaded in sparse mode, multiplied out, give the
+    reference's interpolation matrix ``p``: same pattern, values within
+    single-precision rounding of the per-axis factors."""
+    c = dict(cases.sparse_cases())[name]
+    g = cases.load("sparse_cases")
+    A = host_nufft(**c["kw"])
+    assert A.plan.weights is not None
+    w_re, w_im = A.plan.weights
+    assert len(w_re) == 2 and w_re[0].shape == (A.M, A.Jd[0])
+    assert (w_im is None) == (c["kw"]["phasing"] == "real")
+    p = A.p.tocsc()
+    p.sort_indices()
+    np.testing.assert_array_equal(p.indptr, g[name + "_p_indptr"])
+    np.testing.assert_array_equal(p.indices, g[name + "_p_indices"])
+    tol = 1e-6 if c["kw"]["precision"] == "single" else 1e-13
+    assert rel_l2(p.data, g[name + "_p_data"]) < tol
+
+
+def test_sparse_mode_rejects_unknown_mode(host_nufft):
+    c = cases.radial_2d_128()
+    kw = dict(c["kw"])
+    kw["mode"] = "lut"
+    with pytest.raises(ValueError):
+        host_nufft(**kw)
