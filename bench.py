@@ -341,6 +341,12 @@ def run_ours(args, rank, world):
         xa_or = B.adj(y_gpu.reshape(y_or.shape))
         xa_gpu = xa_dev[:npar].cpu().numpy().transpose(tuple(range(nd, -1, -1)))
         parity["adj_rel_err_vs_oracle"] = oracle.rel_l2(xa_gpu.reshape(xa_or.shape), xa_or)
+        # both single-precision adjoints against the oracle in double precision:
+        # dense trajectory centres make float32 sums order-dependent
+        B64 = oracle.OracleNufft(**dict(kw, precision="double"))
+        xa_64 = B64.adj(y_gpu.reshape(y_or.shape).astype(np.complex128))
+        parity["adj_rel_err_vs_fp64_oracle"] = oracle.rel_l2(xa_gpu.reshape(xa_64.shape), xa_64)
+        parity["oracle_adj_rel_err_vs_fp64_oracle"] = oracle.rel_l2(xa_or.reshape(xa_64.shape), xa_64)
         rows = np.random.default_rng(0).choice(M, 4096 if nd < 3 else 1024, replace=False)
         y_ex = dtft(x_f[..., 0].astype(np.complex128), omega[rows], shape=w["Nd"])
         y_or0 = y_or.reshape(M, -1)[:, 0]

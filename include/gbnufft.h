@@ -44,6 +44,13 @@ extern "C" {
 #define GBN_PHASING_REAL 0
 #define GBN_PHASING_COMPLEX 1
 
+/* Geometry flags.  By default a plan precomputes every sample's table
+ * coefficients once (list order, jsum = sum(Jd) values per sample and per
+ * spread-list entry) and the kernels read them; TABLE_ONLY keeps no such
+ * buffers and interpolates the tables inside the kernels instead (same
+ * results bit for bit, less device memory).                               */
+#define GBN_FLAG_TABLE_ONLY 1
+
 /* Geometry of one operator (or of a series of frames sharing it). */
 typedef struct gbn_geometry {
     int ndim;              /* 1, 2 or 3                                       */
@@ -65,7 +72,7 @@ typedef struct gbn_geometry {
     int tile[3];           /* gather tile edge per memory axis, 0 = default   */
     int stile[3];          /* spread tile edge per memory axis, 0 = default   */
     int max_coils;         /* largest coil count a call will use              */
-    int flags;             /* reserved, 0                                     */
+    int flags;             /* GBN_FLAG_* bits, 0 by default                   */
 } gbn_geometry;
 
 typedef struct gbn_plan gbn_plan;

@@ -18,6 +18,8 @@ GBN_ERR_NOMEM = 4
 GBN_ERR_UNSUPPORTED = 5
 GBN_ERR_TOOLARGE = 6
 
+FLAG_TABLE_ONLY = 1
+
 PRECISION = {"single": 0, "double": 1}
 PHASING = {"real": 0, "complex": 1}
 

@@ -360,10 +360,14 @@ class NufftBase(object):
             t = t.permute(*reversed(range(len(full)))).contiguous()
         else:
             arr = np.asfortranarray(arr.reshape(full, order="F") if arr.shape != full else arr)
+            # one host-to-device copy straight from the caller's memory (no
+            # pinned staging copy: host memory is directly reachable by the
+            # copy engines at full speed on Grace-Blackwell, and arrays this
+            # operator returned are pinned already)
             host = torch.from_numpy(arr.ravel(order="F"))
-            if torch.cuda.is_available():
-                host = host.pin_memory()
-            t = host.to(dev, non_blocking=True).reshape(tuple(reversed(full)))
+            # asynchronous only when the call ends with a stream synchronisation
+            # (host outputs), so the caller may reuse its array on return
+            t = host.to(dev, non_blocking=not self.on_gpu).reshape(tuple(reversed(full)))
         return t, reps
 
     def _device_out(self, t, reps, leading_shape):
@@ -373,7 +377,13 @@ class NufftBase(object):
         if self.on_gpu:
             out = t.permute(*reversed(range(nd)))
         else:
-            out = t.cpu().numpy().transpose(tuple(reversed(range(nd))))
+            # pinned result buffer from torch's caching host allocator: no
+            # first-touch page faults on a fresh allocation, full-speed copy;
+            # the returned array keeps the buffer alive
+            host = torch.empty(t.shape, dtype=t.dtype, pin_memory=True)
+            host.copy_(t, non_blocking=True)
+            torch.cuda.current_stream(t.device).synchronize()
+            out = host.numpy().transpose(tuple(reversed(range(nd))))
         if reps == 1:
             out = out[..., 0]
         return out

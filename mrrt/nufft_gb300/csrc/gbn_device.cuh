@@ -66,6 +66,14 @@ __device__ __forceinline__ typename Cx<R>::T phase_before(const Geom<R>& g, cons
     return cmake<R>(cs, sn);
 }
 
+// (1 - alf) h0 + alf h1 with both products and the sum rounded separately
+// (no contraction into a fused multiply-add), as the reference's C
+// evaluates it: the same bits wherever the compiler inlines it.
+template <typename R>
+__device__ __forceinline__ R lerp_rn(R alf, R h0, R h1) {
+    return add_rn(mul_rn((R)1 - alf, h0), mul_rn(alf, h1));
+}
+
 // Linearly interpolated table coefficient for tap k of coordinate t
 // (nufft_table.template.c:581-585):  p = (t - k) L, n = floor(p),
 // coef = (1 - alf) h[n] + alf h[n + 1].  Tables are zero-padded by two
@@ -80,27 +88,12 @@ __device__ __forceinline__ void table_coef(const Geom<R>& g, int d, R t, int k, 
     const int n = min(max((int)nf + g.ncenter[d], -2), g.J[d] * g.L + 1);
     const R alf = pp - nf;
     const R* h = g.hr[d];
-    cr = ((R)1 - alf) * __ldg(h + n) + alf * __ldg(h + n + 1);
+    cr = lerp_rn(alf, __ldg(h + n), __ldg(h + n + 1));
     if (CX) {
         const R* hi = g.hi[d];
-        ci = ((R)1 - alf) * __ldg(hi + n) + alf * __ldg(hi + n + 1);
+        ci = lerp_rn(alf, __ldg(hi + n), __ldg(hi + n + 1));
     } else {
         ci = (R)0;
-    }
-}
-
-// Coefficient of tap j (0 <= j < J) of sample `gs` (index in sample order)
-// on axis d: the precomputed weight in sparse-matrix mode, else the table
-// interpolation at t for tap k = first tap + j.
-template <typename R, bool CX>
-__device__ __forceinline__ void tap_coef(const Geom<R>& g, int d, R t, int kf, int j, int64_t gs, R& cr,
-                                         R& ci) {
-    if (g.wr[0]) {
-        const int64_t w = gs * g.J[d] + j;
-        cr = __ldg(g.wr[d] + w);
-        ci = CX ? __ldg(g.wi[d] + w) : (R)0;
-    } else {
-        table_coef<R, CX>(g, d, t, kf + j, cr, ci);
     }
 }
 

@@ -27,6 +27,33 @@ namespace gbn {
 
 constexpr int GATHER_THREADS = 256;
 
+// Read one entry's precomputed coefficients (jsum values: the taps of axis
+// 0, then axis 1, ...) into per-axis register arrays; 16-byte loads when the
+// width is fixed and the entry size is a multiple of 16 bytes.
+template <typename R, int NDIM, int JJ, int JL>
+__device__ __forceinline__ void load_coefs(const R* src, const Geom<R>& g, R (&c)[NDIM][JL]) {
+    if (JJ > 0 && sizeof(R) == 4 && (NDIM * JJ) % 4 == 0) {
+        constexpr int NV = (JJ > 0 ? NDIM * JJ : 4) / 4;
+        float4 v[NV];
+#pragma unroll
+        for (int i = 0; i < NV; ++i) v[i] = __ldg(reinterpret_cast<const float4*>(src) + i);
+        const float* f = reinterpret_cast<const float*>(v);
+#pragma unroll
+        for (int d = 0; d < NDIM; ++d)
+#pragma unroll
+            for (int j = 0; j < JL; ++j) c[d][j] = (R)f[d * JJ + j];
+    } else {
+        int off = 0;
+#pragma unroll
+        for (int d = 0; d < NDIM; ++d) {
+#pragma unroll
+            for (int j = 0; j < JL; ++j)
+                if (JJ > 0 || j < g.J[d]) c[d][j] = __ldg(src + off + j);
+            off += JJ > 0 ? JJ : g.J[d];
+        }
+    }
+}
+
 template <typename R, int NDIM, bool CX, int JJ, int LSC>
 __global__ void __launch_bounds__(GATHER_THREADS)
 gather_kernel(const GatherParams<R> p) {
@@ -120,16 +147,25 @@ gather_kernel(const GatherParams<R> p) {
         if (lane < nb) {
             const int e = start + base + lane;
             midx = p.s.idx[e];
-            const int64_t gs = fo + midx;
             int loc[3] = {0, 0, 0};
+            R tt[3];
+            int kf[3];
 #pragma unroll
             for (int d = 0; d < NDIM; ++d) {
-                const R t = p.s.t[d][e];
-                const int kf = first_tap(t, g.J[d]);
-                loc[d] = wrapk(kf, g.K[d]) - org[d];
+                tt[d] = p.s.t[d][e];
+                kf[d] = first_tap(tt[d], g.J[d]);
+                loc[d] = wrapk(kf[d], g.K[d]) - org[d];
+            }
+            if (p.s.cr) {
+                // precomputed coefficients: jsum contiguous values per entry
+                load_coefs<R, NDIM, JJ, JL>(p.s.cr + (int64_t)e * p.s.jsum, g, mcr);
+                if (CX) load_coefs<R, NDIM, JJ, JL>(p.s.ci + (int64_t)e * p.s.jsum, g, mci);
+            } else {
 #pragma unroll
-                for (int j = 0; j < JL; ++j)
-                    if (JJ > 0 || j < g.J[d]) tap_coef<R, CX>(g, d, t, kf, j, gs, mcr[d][j], mci[d][j]);
+                for (int d = 0; d < NDIM; ++d)
+#pragma unroll
+                    for (int j = 0; j < JL; ++j)
+                        if (JJ > 0 || j < g.J[d]) table_coef<R, CX>(g, d, tt[d], kf[d] + j, mcr[d][j], mci[d][j]);
             }
             mbase = ((loc[2] * Rd[1] + loc[1]) * Rd[0] + loc[0]) * LSP;
             if (p.apply_ph) mph = p.s.ph[e];

@@ -47,7 +47,7 @@ __global__ void __launch_bounds__(128) grad_kernel(const GradParams<R> p) {
                 const R nf = floor(pp);
                 const int n = min(max((int)nf + g.ncenter[d], -2), g.J[d] * g.L + 1);
                 const R alf = pp - nf;
-                dc[d][j] = ((R)1 - alf) * __ldg(p.dh[d] + n) + alf * __ldg(p.dh[d] + n + 1);
+                dc[d][j] = lerp_rn(alf, __ldg(p.dh[d] + n), __ldg(p.dh[d] + n + 1));
             }
         }
     }

@@ -34,11 +34,6 @@ struct Geom {
     int ncenter[3];          // floor(J*L/2): table index of t = 0
     const R* hr[3];          // device tables (shifted past their zero padding)
     const R* hi[3];          // imaginary tables, nullptr for a real kernel
-    // Precomputed interpolation weights (sparse-matrix mode): per axis
-    // [M_total][J] in sample order (frame offset + index), used instead of
-    // the tables when wr[0] is set; wi imaginary parts or nullptr.
-    const R* wr[3];
-    const R* wi[3];
     int64_t Kprod, Nprod;
     R pbc[3];                // phase_before coefficient per memory axis
     int pbo[3];              // summation order of the per-axis phases
@@ -58,6 +53,32 @@ struct SampleList {
     const int* idx;                 // sample index within its frame
     const typename Cx<R>::T* ph;    // per-sample phase (list order) or nullptr
     const short4* ls;               // spread list: window start in tile coordinates
+    // Interpolation coefficients precomputed in list order, or nullptr (the
+    // kernels then interpolate the tables): entry e holds jsum values, the
+    // J_0 taps of axis 0, then the J_1 taps of axis 1, ...; ci the imaginary
+    // parts for a complex kernel.
+    const R* cr;
+    const R* ci;
+    int jsum;
+};
+
+// Fill a list's precomputed coefficients, for every entry of every work
+// item: from the tables (bitwise the values the kernels would interpolate)
+// or, in sparse-matrix mode, from per-sample weights wr[d] / wi[d]
+// ([M_total][J_d], sample order = frame offset + index).
+template <typename R>
+struct CoefParams {
+    Geom<R> g;
+    SampleList<R> s;
+    const int4* items;              // {frame, tile, start, count}
+    int nitems;
+    const int64_t* foff;
+    const R* wr[3];
+    const R* wi[3];
+    R* out_r;
+    R* out_i;
+    int jsum;
+    int cx;
 };
 
 template <typename R>
@@ -153,6 +174,7 @@ template <typename R> cudaError_t launch_reduce(const ReduceParams<R>& p, cudaSt
 template <typename R> cudaError_t launch_pad(const PadParams<R>& p, cudaStream_t s);
 template <typename R> cudaError_t launch_crop(const CropParams<R>& p, cudaStream_t s);
 template <typename R> cudaError_t launch_grad(const GradParams<R>& p, cudaStream_t s);
+template <typename R> cudaError_t launch_coef(const CoefParams<R>& p, cudaStream_t s);
 
 // Shared-memory bytes needed by the gather / spread kernels for a lane layout.
 template <typename R> size_t gather_smem(const Geom<R>& g, const Lanes& ln);

@@ -144,6 +144,8 @@ struct gbn_plan {
 
     DevBuf tables, dtables, sn, dfoff;
     DevBuf weights;       // sparse-matrix mode: per-axis [M_total][J] weights (re, then im)
+    DevBuf gcoef, scoef;  // precomputed coefficients in gather / spread list order
+    bool coefs = false;   // gcoef / scoef hold the current lists' coefficients
     DevBuf glist, gitems;
     DevBuf slist, sitems, sparts, rtiles;
     int n_gitems = 0, n_sitems = 0, n_rtiles = 0, n_slots = 0;
@@ -203,18 +205,6 @@ Geom<R> make_geom(const gbn_plan* P, bool spread) {
         g.hi[d] = base + off + 2;
         off += len;
     }
-    if (P->weights.p) {
-        const R* w = reinterpret_cast<const R*>(P->weights.p);
-        size_t woff = 0;
-        for (int d = 0; d < G.ndim; ++d) {
-            g.wr[d] = w + woff;
-            woff += (size_t)P->M_total * G.Jd[d];
-        }
-        for (int d = 0; d < G.ndim && P->cx; ++d) {
-            g.wi[d] = w + woff;
-            woff += (size_t)P->M_total * G.Jd[d];
-        }
-    }
     g.L = G.L;
     g.Kprod = P->Kprod;
     g.Nprod = P->Nprod;
@@ -259,6 +249,14 @@ SampleList<R> make_list(const gbn_plan* P, const DevBuf& buf, int64_t len, bool 
     if (P->has_phase) s.ph = reinterpret_cast<const C*>(b + L.ph);
     for (int d = 0; d < P->geom.ndim; ++d) s.t[d] = reinterpret_cast<const R*>(b + L.t[d]);
     s.idx = reinterpret_cast<const int*>(b + L.idx);
+    if (P->coefs) {
+        const DevBuf& cb = with_ls ? P->scoef : P->gcoef;
+        int jsum = 0;
+        for (int d = 0; d < P->geom.ndim; ++d) jsum += P->geom.Jd[d];
+        s.jsum = jsum;
+        s.cr = reinterpret_cast<const R*>(cb.p);
+        if (P->cx) s.ci = s.cr + (size_t)len * jsum;
+    }
     return s;
 }
 
@@ -835,11 +833,65 @@ int validate(const gbn_geometry* g) {
     return GBN_OK;
 }
 
+// Precompute both lists' interpolation coefficients (list order): from the
+// sparse-mode weights when set, else from the tables unless the geometry
+// asks for table interpolation inside the kernels (GBN_FLAG_TABLE_ONLY).
+template <typename R>
+int fill_coefs(gbn_plan* P) {
+    P->coefs = false;
+    const gbn_geometry& G = P->geom;
+    if (!P->weights.p && (G.flags & GBN_FLAG_TABLE_ONLY)) {
+        GBN_CUDA(P->gcoef.alloc(0), "coefficient release");
+        GBN_CUDA(P->scoef.alloc(0), "coefficient release");
+        return GBN_OK;
+    }
+    int jsum = 0;
+    for (int d = 0; d < G.ndim; ++d) jsum += G.Jd[d];
+    const size_t parts = P->cx ? 2 : 1;
+    const size_t gb = (size_t)P->glen * jsum * parts * sizeof(R);
+    const size_t sb = (size_t)P->slen * jsum * parts * sizeof(R);
+    GBN_CUDA(P->gcoef.alloc(std::max<size_t>(gb, 16)), "gather coefficient allocation");
+    GBN_CUDA(P->scoef.alloc(std::max<size_t>(sb, 16)), "spread coefficient allocation");
+    for (int which = 0; which < 2; ++which) {
+        const bool spread = which == 1;
+        CoefParams<R> c;
+        std::memset(&c, 0, sizeof(c));
+        c.g = make_geom<R>(P, spread);
+        c.s = make_list<R>(P, spread ? P->slist : P->glist, spread ? P->slen : P->glen, spread);
+        c.items = reinterpret_cast<const int4*>(spread ? P->sitems.p : P->gitems.p);
+        c.nitems = spread ? P->n_sitems : P->n_gitems;
+        c.foff = reinterpret_cast<const int64_t*>(P->dfoff.p);
+        if (P->weights.p) {
+            const R* w = reinterpret_cast<const R*>(P->weights.p);
+            size_t woff = 0;
+            for (int d = 0; d < G.ndim; ++d) {
+                c.wr[d] = w + woff;
+                woff += (size_t)P->M_total * G.Jd[d];
+            }
+            for (int d = 0; d < G.ndim && P->cx; ++d) {
+                c.wi[d] = w + woff;
+                woff += (size_t)P->M_total * G.Jd[d];
+            }
+        }
+        const int64_t len = spread ? P->slen : P->glen;
+        c.out_r = reinterpret_cast<R*>(spread ? P->scoef.p : P->gcoef.p);
+        c.out_i = P->cx ? c.out_r + (size_t)len * jsum : nullptr;
+        c.jsum = jsum;
+        c.cx = P->cx ? 1 : 0;
+        GBN_CUDA(launch_coef<R>(c, 0), "coefficient launch");
+    }
+    GBN_CUDA(cudaDeviceSynchronize(), "coefficient precompute");
+    P->coefs = true;
+    return GBN_OK;
+}
+
 template <typename R>
 int plan_points(gbn_plan* P, const void* tm, const void* phase) {
     if (!tm && P->M_total > 0) return fail(GBN_ERR_INVALID, "null coordinate array");
     P->has_phase = phase != nullptr;
-    return build_lists<R>(P, reinterpret_cast<const R*>(tm), reinterpret_cast<const R*>(phase));
+    int rc = build_lists<R>(P, reinterpret_cast<const R*>(tm), reinterpret_cast<const R*>(phase));
+    if (rc) return rc;
+    return fill_coefs<R>(P);
 }
 
 }  // namespace
@@ -1034,7 +1086,7 @@ int gbn_plan_set_weights(gbn_plan* P, const void* const* w_re, const void* const
     GBN_CUDA(cudaDeviceSynchronize(), "synchronise before replacing weights");
     if (!w_re) {
         GBN_CUDA(P->weights.alloc(0), "weight release");
-        return GBN_OK;
+        return P->dbl ? fill_coefs<double>(P) : fill_coefs<float>(P);
     }
     const gbn_geometry& G = P->geom;
     if (P->cx && !w_im) return fail(GBN_ERR_INVALID, "complex phasing needs imaginary weights");
@@ -1055,7 +1107,7 @@ int gbn_plan_set_weights(gbn_plan* P, const void* const* w_re, const void* const
                      "weight upload");
             off += n;
         }
-    return GBN_OK;
+    return P->dbl ? fill_coefs<double>(P) : fill_coefs<float>(P);
 }
 
 int gbn_grad_tm(gbn_plan* P, const void* grid, const void* gy, const double* phase_shift, void* gtm,
@@ -1104,7 +1156,7 @@ int gbn_plan_stats(const gbn_plan* P, int64_t* o) {
     o[3] = P->glen;
     o[4] = P->slen;
     o[5] = (int64_t)P->ntiles_s * P->F;
-    o[6] = (int64_t)(P->tables.bytes + P->weights.bytes + P->sn.bytes + P->glist.bytes + P->slist.bytes + P->pad.bytes +
+    o[6] = (int64_t)(P->tables.bytes + P->weights.bytes + P->gcoef.bytes + P->scoef.bytes + P->sn.bytes + P->glist.bytes + P->slist.bytes + P->pad.bytes +
                      P->grid.bytes + P->scratch.bytes);
     o[7] = P->M_total;
     return GBN_OK;

@@ -39,6 +39,72 @@ struct SpreadLayout {
     static constexpr int PSTR = PSUM + 1;
 };
 
+// One staged entry's contribution to a warp's register block: its value
+// for this lane's coil and the block's slice of its coefficient rows
+// (loaded), then B0 x B1 x B2 multiply-adds (accumulate).
+template <typename R, int NDIM, bool CX, typename SL>
+struct EntryOps {
+    typedef typename Cx<R>::T C;
+    static constexpr int B0 = SL::B0, B1 = SL::B1, B2 = SL::B2;
+    C v;
+    C a0[B0], a1[B1], a2[B2];
+
+    __device__ __forceinline__ void load(const C* cp, const C* vb, const short4* sls, int el, int VS, int coil,
+                                         int bo0, int bo1, int bo2) {
+        const short4 s = sls[el];
+        v = vb[el * VS + coil];
+        const C* row = cp + el * SL::PSTR;
+        const int i0 = bo0 - s.x + (B0 - 1);
+#pragma unroll
+        for (int k = 0; k < B0; ++k) a0[k] = row[i0 + k];
+        if (NDIM > 1) {
+            const int i1 = SL::P0 + bo1 - s.y + (B1 - 1);
+#pragma unroll
+            for (int k = 0; k < B1; ++k) a1[k] = row[i1 + k];
+        } else {
+            a1[0] = CX ? cmake<R>((R)1, (R)0) : cmake<R>((R)1, (R)1);   // neutral factor
+        }
+        if (NDIM > 2) {
+            const int i2 = SL::P0 + SL::P1 + bo2 - s.z + (B2 - 1);
+#pragma unroll
+            for (int k = 0; k < B2; ++k) a2[k] = row[i2 + k];
+        } else {
+            a2[0] = CX ? cmake<R>((R)1, (R)0) : cmake<R>((R)1, (R)1);
+        }
+    }
+
+    template <int NB>
+    __device__ __forceinline__ void accumulate(C (&acc)[NB]) const {
+#pragma unroll
+        for (int k2 = 0; k2 < B2; ++k2) {
+#pragma unroll
+            for (int k1 = 0; k1 < B1; ++k1) {
+                C tv;
+                if (CX) {
+                    // conj(c2 c1) v, the pairs already hold conj
+                    const C w = cmul(a1[k1], a2[k2]);
+                    tv = cmul(w, v);
+                } else {
+                    // pairs (c, c): w12 = c1 c2 on both halves, tv = w12 v
+                    const C w12 = NDIM > 2 ? pmul(a1[k1], a2[k2]) : a1[k1];
+                    tv = pmul(w12, v);
+                }
+#pragma unroll
+                for (int k0 = 0; k0 < B0; ++k0) {
+                    const int q = (k2 * B1 + k1) * B0 + k0;
+                    if (CX) {
+                        const C w0 = cmul(a0[k0], tv);
+                        acc[q].x += w0.x;
+                        acc[q].y += w0.y;
+                    } else {
+                        acc[q] = pfma(a0[k0], tv, acc[q]);
+                    }
+                }
+            }
+        }
+    }
+};
+
 int spread_threads(int ndim, const int* T) {
     int b[3];
     if (ndim == 1) { b[0] = SpreadBlock<1>::B0; b[1] = b[2] = 1; }
@@ -50,7 +116,7 @@ int spread_threads(int ndim, const int* T) {
 }
 
 template <typename R, int NDIM, bool CX, int JJ, int LSC>
-__global__ void __launch_bounds__(256, 3)
+__global__ void __launch_bounds__(256, 4)
 spread_kernel(const SpreadParams<R> p) {
     typedef typename Cx<R>::T C;
     typedef SpreadLayout<NDIM> SL;
@@ -155,8 +221,11 @@ spread_kernel(const SpreadParams<R> p) {
         }
         for (int q = tid; q < n; q += nthr) {
             cp_async<sizeof(short4)>(lsb + b * CH + q, p.s.ls + e0 + q);
+            if (!p.s.cr) {
 #pragma unroll
-            for (int d = 0; d < NDIM; ++d) cp_async<sizeof(R)>(tb + (b * NDIM + d) * CH + q, p.s.t[d] + e0 + q);
+                for (int d = 0; d < NDIM; ++d)
+                    cp_async<sizeof(R)>(tb + (b * NDIM + d) * CH + q, p.s.t[d] + e0 + q);
+            }
         }
         cp_async_commit();
     };
@@ -203,10 +272,15 @@ spread_kernel(const SpreadParams<R> p) {
                     Jd = Jz;
                 }
             }
-            const R t = tb[(b * NDIM + d) * CH + el];
-            R cr, ci;
-            const int64_t gs = g.wr[0] ? fo + p.s.idx[start + k * CH + el] : 0;
-            tap_coef<R, CX>(g, d, t, first_tap(t, Jd), j, gs, cr, ci);
+            R cr, ci = (R)0;
+            if (p.s.cr) {
+                const int64_t ce = (int64_t)(start + k * CH + el) * Jsum + (q - el * Jsum);
+                cr = p.s.cr[ce];
+                if (CX) ci = p.s.ci[ce];
+            } else {
+                const R t = tb[(b * NDIM + d) * CH + el];
+                table_coef<R, CX>(g, d, t, first_tap(t, Jd) + j, cr, ci);
+            }
             cp[el * SL::PSTR + slot0 + j] = CX ? cmake<R>(cr, -ci) : cmake<R>(cr, cr);
         }
         // ---- copy-in of chunk k+1 overlaps with the accumulation of chunk k ----
@@ -229,7 +303,9 @@ spread_kernel(const SpreadParams<R> p) {
             }
             unsigned mask = __ballot_sync(0xffffffffu, hit);
             while (mask) {
-                // slot k takes the k-th remaining hit, in entry order
+                // slot k takes the k-th and (k + SW)-th remaining hits and
+                // accumulates them in entry order: two independent load
+                // chains in flight per iteration
                 int pos = -1;
                 for (int kk = 0; kk < SW && mask; ++kk) {
                     const int pk = __ffs(mask) - 1;
@@ -237,55 +313,9 @@ spread_kernel(const SpreadParams<R> p) {
                     if (kk == slot) pos = pk;
                 }
                 if (pos >= 0 && coil < nc) {
-                    const int el = gb + pos;
-                    const short4 s = sls[el];
-                    const C v = vb[el * VS + coil];
-                    const C* row = cp + el * SL::PSTR;
-                    C a0[B0], a1[B1], a2[B2];
-                    const int i0 = bo0 - s.x + (B0 - 1);
-#pragma unroll
-                    for (int k = 0; k < B0; ++k) a0[k] = row[i0 + k];
-                    if (NDIM > 1) {
-                        const int i1 = SL::P0 + bo1 - s.y + (B1 - 1);
-#pragma unroll
-                        for (int k = 0; k < B1; ++k) a1[k] = row[i1 + k];
-                    } else {
-                        a1[0] = CX ? cmake<R>((R)1, (R)0) : cmake<R>((R)1, (R)1);   // neutral factor
-                    }
-                    if (NDIM > 2) {
-                        const int i2 = SL::P0 + SL::P1 + bo2 - s.z + (B2 - 1);
-#pragma unroll
-                        for (int k = 0; k < B2; ++k) a2[k] = row[i2 + k];
-                    } else {
-                        a2[0] = CX ? cmake<R>((R)1, (R)0) : cmake<R>((R)1, (R)1);
-                    }
-#pragma unroll
-                    for (int k2 = 0; k2 < B2; ++k2) {
-#pragma unroll
-                        for (int k1 = 0; k1 < B1; ++k1) {
-                            C tv;
-                            if (CX) {
-                                // conj(c2 c1) v, the pairs already hold conj
-                                const C w = cmul(a1[k1], a2[k2]);
-                                tv = cmul(w, v);
-                            } else {
-                                // pairs (c, c): w12 = c1 c2 on both halves, tv = w12 v
-                                const C w12 = NDIM > 2 ? pmul(a1[k1], a2[k2]) : a1[k1];
-                                tv = pmul(w12, v);
-                            }
-#pragma unroll
-                            for (int k0 = 0; k0 < B0; ++k0) {
-                                const int q = (k2 * B1 + k1) * B0 + k0;
-                                if (CX) {
-                                    const C w0 = cmul(a0[k0], tv);
-                                    acc[q].x += w0.x;
-                                    acc[q].y += w0.y;
-                                } else {
-                                    acc[q] = pfma(a0[k0], tv, acc[q]);
-                                }
-                            }
-                        }
-                    }
+                    EntryOps<R, NDIM, CX, SL> A;
+                    A.load(cp, vb, sls, gb + pos, VS, coil, bo0, bo1, bo2);
+                    A.accumulate(acc);
                 }
             }
         }
