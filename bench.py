@@ -8,8 +8,10 @@ Inputs are seeded synthetic data (complex N(0,1) image times smooth Gaussian
 coil maps); no dataset is involved.
 
 Reported (one JSON line on rank 0):
-  value      batched coil-pairs/s with inputs resident in HBM (CUDA events,
-             L2 flushed between steps by a 256 MB write)
+  value      batched coil-pairs/s with inputs resident in HBM, the step
+             (batched forward + adjoint) replayed from a CUDA graph (CUDA
+             events, L2 flushed between steps by a 256 MB write); "eager"
+             holds the same step launched call by call
   e2e        the same metric through the public drop-in API with host numpy
              buffers (H2D and D2H inside the timed region)
   per_call   coil-pairs/s of the plain per-coil transform on the same GPU
@@ -48,6 +50,9 @@ WORKLOADS = {
     # 3-D kooshball: interp3 gather and 3-D tiled spread
     "3d-kooshball": dict(name="3d-kooshball", kind="koosh3d", Nd=(128, 128, 128), Kd=(256, 256, 256),
                          Jd=(6, 6, 6), L=1024, spokes=12000, readout=256, coils=8),
+    # the 3-D kernels on a smaller volume (inputs still larger than L2), for profiler captures
+    "3d-kooshball-96": dict(name="3d-kooshball-96", kind="koosh3d", Nd=(96, 96, 96), Kd=(192, 192, 192),
+                            Jd=(6, 6, 6), L=1024, spokes=6000, readout=192, coils=8),
     # uneven dynamic series: every frame and coil in one launch per stage, CUDA graph, autotuned tiles
     "series-2d": dict(name="series-2d", kind="series", Nd=(192, 192), Kd=(384, 384), Jd=(6, 6),
                       L=1024, frames=64, readout=384, min_spokes=13, max_spokes=89, seed=4, coils=8),
@@ -356,16 +361,27 @@ def run_ours(args, rank, world):
     stats = P.stats()
     launches_per_step = 2 + 2 + (1 if stats["split_tiles"] > 0 else 0)
 
-    # ---- batched, device resident ------------------------------------------
+    # ---- batched, device resident: the step replayed from a CUDA graph -----
     for _ in range(args.warmup):
         pair()
+    torch.cuda.synchronize()
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph):
+        pair()
+
+    def pair_graph():
+        graph.replay()
+
+    for _ in range(args.warmup):
+        pair_graph()
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
     sampler = clock_sampler_start(_clock_path(rank)) if rank == 0 else None
-    t_batched = time_events(pair, args.steps, flush)
+    t_batched = time_events(pair_graph, args.steps, flush)
     torch.cuda.synchronize()
     t_batched = max_over_ranks(t_batched, world, dev)
+    t_eager = time_events(pair, args.steps, flush) / args.steps
 
     # ---- per-kernel timing for the roofline (same kernels, alone) -----------
     grid = torch.empty((C, Kp), dtype=torch.complex64, device=dev)
@@ -428,7 +444,8 @@ def run_ours(args, rank, world):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "complex64", "data": "synthetic",
-        "config": config_dict(),
+        "config": config_dict({"graph": True}),
+        "eager": {"ms_per_step": t_eager, "value": C / (t_eager * 1e-3)},
         "per_call": {"value": C / (t_percall * 1e-3), "unit": UNIT, "ms_per_step": t_percall,
                      "calls_per_step": 2 * C,
                      "batched_over_per_call": (C / (ms_per_step * 1e-3)) / (C / (t_percall * 1e-3))},
