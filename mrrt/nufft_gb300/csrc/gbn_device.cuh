@@ -119,23 +119,6 @@ __device__ __forceinline__ int region_dims(const Geom<R>& g, int ndim, int* Rd) 
     return tot;
 }
 
-// Complex FMA helpers: acc += c * v with c = (cr, ci) (ci == 0 when !CX).
-template <bool CX, typename C, typename R>
-__device__ __forceinline__ void cfma(C& acc, R cr, R ci, C v);
-// acc += conj(c) * v
-template <bool CX, typename C, typename R>
-__device__ __forceinline__ C cscale_conj(R cr, R ci, C v) {
-    C r;
-    r.x = cr * v.x;
-    r.y = cr * v.y;
-    if (CX) {
-        r.x += ci * v.y;
-        r.y -= ci * v.x;
-    }
-    return r;
-}
-
-
 // Packed single-precision pairs (Blackwell f32x2 pipe): one instruction for
 // two IEEE round-to-nearest operations, bitwise identical to two scalar
 // fmaf / multiplications.
@@ -158,27 +141,6 @@ __device__ __forceinline__ float2 fmul2(float2 a, float2 b) {
     asm("mov.b64 {%0, %1}, %2;" : "=f"(d.x), "=f"(d.y) : "l"(rd));
     return d;
 }
-// c * v + acc for real c and complex v, acc (pair ops in single precision)
-__device__ __forceinline__ float2 rcfma(float c, float2 v, float2 acc) { return ffma2(make_float2(c, c), v, acc); }
-__device__ __forceinline__ double2 rcfma(double c, double2 v, double2 acc) {
-    return make_double2(fma(c, v.x, acc.x), fma(c, v.y, acc.y));
-}
-__device__ __forceinline__ float2 rcmul(float c, float2 v) { return fmul2(make_float2(c, c), v); }
-__device__ __forceinline__ double2 rcmul(double c, double2 v) { return make_double2(c * v.x, c * v.y); }
-
-template <bool CX, typename C, typename R>
-__device__ __forceinline__ void cfma(C& acc, R cr, R ci, C v) {
-    if (CX) {
-        acc.x += cr * v.x;
-        acc.y += cr * v.y;
-        acc.x -= ci * v.y;
-        acc.y += ci * v.x;
-    } else {
-        acc = rcfma(cr, v, acc);
-    }
-}
-
-
 // Asynchronous global -> shared copies (cp.async, cached in L1 and L2).
 // BYTES is 4, 8 or 16; both addresses must be aligned to BYTES.
 template <int BYTES>

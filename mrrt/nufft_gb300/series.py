@@ -68,9 +68,12 @@ class NufftSeries(object):
                 om = om[:, None]
             if om.shape[1] != ndim:
                 raise ValueError("number of cols must match NUFFT dimension")
-            om = om.astype(rdt)
-            tms.append(normalised_coordinates(om, Kd, rdt))
+            if om.dtype not in (np.float32, np.float64):
+                om = om.astype(np.float64)
+            # as NufftBase: the phase from omega in its given dtype, the
+            # coordinates from omega cast to the operator's real dtype
             phases.append(sample_phase_of(om, n_shift, self.n_mid, "real", rdt, cdt))
+            tms.append(normalised_coordinates(om.astype(rdt), Kd, rdt))
             counts.append(om.shape[0])
         if not counts:
             raise ValueError("a series needs at least one frame")

@@ -17,6 +17,8 @@ class _RecordingPlan:
         self.args = dict(Nd=Nd, Kd=Kd, Jd=Jd, L=L, rdt=rdt, tables_re=tables_re, tables_im=tables_im,
                          sn=sn, tm=tm, sample_phase=sample_phase, **kw)
         self.weights = None
+        self.ctype = None
+        self.device = None
 
     def set_weights(self, w_re, w_im=None):
         self.weights = (w_re, w_im)
@@ -70,3 +72,45 @@ def test_sparse_mode_rejects_unknown_mode(host_nufft):
     kw["mode"] = "lut"
     with pytest.raises(ValueError):
         host_nufft(**kw)
+
+
+def test_series_plan_concatenates_frames(monkeypatch, host_nufft):
+    """NufftSeries uploads one plan holding every frame: frame offsets, the
+    frames' coordinates and phases in order, each equal to what a
+    single-frame operator would upload."""
+    from mrrt.nufft_gb300 import series
+    from mrrt.nufft_gb300.trajectories import uneven_series_2d
+
+    monkeypatch.setattr(series, "require_cuda", lambda: None)
+    monkeypatch.setattr(series, "GpuPlan", _RecordingPlan)
+    oms = uneven_series_2d(5, 64, min_spokes=3, max_spokes=9, seed=2)
+    S = series.NufftSeries((32, 32), oms, Jd=(6, 6), Kd=(64, 64), coils=4)
+    counts = [o.shape[0] for o in oms]
+    np.testing.assert_array_equal(S.frame_offsets, np.concatenate([[0], np.cumsum(counts)]))
+    up = S.plan.args
+    assert up["frame_offsets"] is S.frame_offsets and up["max_coils"] == 4
+    for f, om in enumerate(oms):
+        A = host_nufft((32, 32), om, Jd=(6, 6), Kd=(64, 64))
+        a, b = S.frame_offsets[f], S.frame_offsets[f + 1]
+        np.testing.assert_array_equal(up["tm"][a:b], A.plan.args["tm"])
+        np.testing.assert_array_equal(up["sample_phase"][a:b], A.plan.args["sample_phase"])
+    np.testing.assert_array_equal(up["sn"], A.plan.args["sn"])
+
+
+def test_autotune_cache_round_trip(tmp_path):
+    from mrrt.nufft_gb300 import autotune
+
+    path = str(tmp_path / "tune.json")
+    key = autotune._key("series", (64, 64), (128, 128), (6, 6), [10, 20], 4, "single")
+    assert autotune._load(path) == {}
+    autotune._store(path, key, {"tile": [32, 16], "stile": [8, 8], "report": {}})
+    autotune._store(path, key + "x", {"tile": [16, 8], "stile": [16, 8], "report": {}})
+    got = autotune._load(path)
+    assert got[key]["tile"] == [32, 16] and got[key + "x"]["stile"] == [16, 8]
+    g2, s2 = autotune.candidate_tiles(2)
+    g3, s3 = autotune.candidate_tiles(3)
+    # spread tiles are whole 4 x 4 (x 1) register blocks, at most 8 per tile
+    for t in s2:
+        assert t[0] % 4 == 0 and t[1] % 4 == 0 and (t[0] // 4) * (t[1] // 4) <= 8
+    for t in s3:
+        assert t[0] % 4 == 0 and t[1] % 4 == 0 and (t[0] // 4) * (t[1] // 4) * t[2] <= 8
