@@ -115,6 +115,22 @@ int gbn_forward(gbn_plan* plan, const void* x, void* y, int coils,
 int gbn_adjoint(gbn_plan* plan, const void* y, void* x, int coils,
                 void* stream);
 
+/* Coil-sensitivity (SENSE) forward: y = NUFFT(maps[c] * image[f]) for every
+ * frame f and coil c, the coil-map multiply fused into the deapodisation
+ * pass (the coil images are never stored).  The MRI system operator of
+ * mrrt.operators, built on the reference's NUFFT, applies maps before
+ * nufft_forward (mrrt/nufft/_nufft.py:3-5 names it); this fuses that step.
+ *   image : [frames][N...]   one image per frame
+ *   maps  : [coils][N...]    coil sensitivities, shared by all frames
+ *   y     : as for gbn_forward.                                             */
+int gbn_forward_sense(gbn_plan* plan, const void* image, const void* maps,
+                      void* y, int coils, void* stream);
+
+/* Coil-combining adjoint: image[f] = sum_c conj(maps[c]) * adjoint_c, the
+ * sum (in coil order) fused into the crop pass.                             */
+int gbn_adjoint_sense(gbn_plan* plan, const void* y, const void* maps,
+                      void* image, int coils, void* stream);
+
 /* Table interpolation alone: oversampled grid -> samples, no phases, no FFT.
  * Replaces interp{1,2,3}_table (mrrt/nufft/_interp_table.py:26-159).        */
 int gbn_interp_forward(gbn_plan* plan, const void* grid, void* y, int coils,

@@ -72,6 +72,8 @@ SIGNATURES = {
     "gbn_interp_adjoint": [_VP, _VP, _VP, _I, _VP],
     "gbn_interp_adjoint_noalloc": [_VP, _VP, _VP, _I, _VP],
     "gbn_plan_set_weights": [_VP, _VP, _VP],
+    "gbn_forward_sense": [_VP, _VP, _VP, _VP, _I, _VP],
+    "gbn_adjoint_sense": [_VP, _VP, _VP, _VP, _I, _VP],
     "gbn_plan_set_dtables": [_VP, ctypes.POINTER(_VP)],
     "gbn_grad_tm": [_VP, _VP, _VP, ctypes.POINTER(ctypes.c_double), _VP, _I, _VP],
     "gbn_forward_grid": [_VP, ctypes.POINTER(_VP)],

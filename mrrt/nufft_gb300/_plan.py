@@ -127,6 +127,32 @@ class GpuPlan:
                                             ctypes.c_void_p(x.data_ptr()), int(coils), _stream()))
         return x
 
+    def forward_sense(self, image, maps, y, coils):
+        """Coil-sensitivity forward: image [F, N...] and maps [coils, N...]
+        (plan layout) -> samples, the map multiply fused into the pad."""
+        F = len(self.frame_offsets) - 1
+        self._check(image, F * self.Nprod, "image")
+        self._check(maps, coils * self.Nprod, "maps")
+        self._check(y, coils * self.M_total, "y")
+        with torch.cuda.device(self.device):
+            _lib.check(self.lib.gbn_forward_sense(self.handle, ctypes.c_void_p(image.data_ptr()),
+                                                  ctypes.c_void_p(maps.data_ptr()),
+                                                  ctypes.c_void_p(y.data_ptr()), int(coils), _stream()))
+        return y
+
+    def adjoint_sense(self, y, maps, image, coils):
+        """Coil-combining adjoint: samples -> image [F, N...] = sum over coils
+        of conj(maps) times each coil's adjoint, fused into the crop."""
+        F = len(self.frame_offsets) - 1
+        self._check(y, coils * self.M_total, "y")
+        self._check(maps, coils * self.Nprod, "maps")
+        self._check(image, F * self.Nprod, "image")
+        with torch.cuda.device(self.device):
+            _lib.check(self.lib.gbn_adjoint_sense(self.handle, ctypes.c_void_p(y.data_ptr()),
+                                                  ctypes.c_void_p(maps.data_ptr()),
+                                                  ctypes.c_void_p(image.data_ptr()), int(coils), _stream()))
+        return image
+
     def interp_forward(self, grid, y, coils):
         F = len(self.frame_offsets) - 1
         self._check(grid, F * coils * self.Kprod, "grid")

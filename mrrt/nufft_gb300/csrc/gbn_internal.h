@@ -137,6 +137,10 @@ struct PadParams {
     const typename Cx<R>::T* x;
     const R* sn;
     typename Cx<R>::T* out;
+    // coil-sensitivity fusion: x is one image per frame [F][N] and plane
+    // f * coils + c receives sn * maps[c] * x[f]; nullptr for the plain pad
+    const typename Cx<R>::T* maps;
+    int coils;
 };
 
 template <typename R>
@@ -149,6 +153,10 @@ struct CropParams {
     const R* sn;
     R scale;
     typename Cx<R>::T* x;
+    // coil combination: x[f] = sum_c conj(maps[c]) * (cropped plane f * coils
+    // + c), one image per frame; nullptr for the plain crop
+    const typename Cx<R>::T* maps;
+    int coils;
 };
 
 template <typename R>

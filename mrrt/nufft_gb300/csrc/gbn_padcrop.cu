@@ -9,7 +9,9 @@
 // (or the orthonormal factors).
 //
 // One warp per image row (memory axis 0); rows are enumerated over
-// (plane, axis 1, axis 2).
+// (plane, axis 1, axis 2).  The coil-sensitivity variants fuse the MRI
+// system operator's coil-map multiply (forward) and conjugate-map coil sum
+// (adjoint) into these passes.
 #include <cuda_runtime.h>
 
 #include "gbn_device.cuh"
@@ -71,6 +73,74 @@ __global__ void __launch_bounds__(256) crop_kernel(const CropParams<R> p) {
     }
 }
 
+// Coil-sensitivity pad: plane f * coils + c gets sn * maps[c] * x[f] (the
+// multiply an MRI system operator applies before the NUFFT, here fused into
+// the deapodisation pass so the coil images are never materialised).
+template <typename R>
+__global__ void __launch_bounds__(256) pad_sense_kernel(const PadParams<R> p) {
+    typedef typename Cx<R>::T C;
+    const int lane = threadIdx.x & 31;
+    const int64_t rows_per_plane = (int64_t)p.N[1] * p.N[2];
+    const int64_t nrows = rows_per_plane * p.planes;
+    const int64_t wid = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t row = wid; row < nrows; row += nw) {
+        const int64_t pl = row / rows_per_plane;
+        const int64_t rr = row - pl * rows_per_plane;
+        const int64_t f = pl / p.coils, c = pl - f * p.coils;
+        const int n1 = (int)(rr % p.N[1]);
+        const int n2 = (int)(rr / p.N[1]);
+        const C* src = p.x + f * p.Nprod + rr * p.N[0];
+        const C* mp = p.maps + c * p.Nprod + rr * p.N[0];
+        const R* s = p.sn + rr * p.N[0];
+        C* dst = p.out + pl * p.Kprod + ((int64_t)n2 * p.K[1] + n1) * p.K[0];
+        for (int n0 = lane; n0 < p.N[0]; n0 += 32) {
+            C v = cmul(src[n0], mp[n0]);
+            const R w = s[n0];
+            v.x *= w;
+            v.y *= w;
+            dst[n0] = v;
+        }
+    }
+}
+
+// Coil-combining crop: x[f] = sum over c (in coil order) of conj(maps[c]) *
+// (scale * sn * cropped plane f * coils + c), one image per frame.
+template <typename R>
+__global__ void __launch_bounds__(256) crop_sense_kernel(const CropParams<R> p) {
+    typedef typename Cx<R>::T C;
+    const int lane = threadIdx.x & 31;
+    const int64_t rows_per_plane = (int64_t)p.N[1] * p.N[2];
+    const int64_t frames = p.planes / p.coils;
+    const int64_t nrows = rows_per_plane * frames;
+    const int64_t wid = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t row = wid; row < nrows; row += nw) {
+        const int64_t f = row / rows_per_plane;
+        const int64_t rr = row - f * rows_per_plane;
+        const int n1 = (int)(rr % p.N[1]);
+        const int n2 = (int)(rr / p.N[1]);
+        const int64_t goff = ((int64_t)n2 * p.K[1] + n1) * p.K[0];
+        const R* s = p.sn + rr * p.N[0];
+        C* dst = p.x + f * p.Nprod + rr * p.N[0];
+        for (int n0 = lane; n0 < p.N[0]; n0 += 32) {
+            const R w = s[n0];
+            C acc = cmake<R>((R)0, (R)0);
+            for (int c = 0; c < p.coils; ++c) {
+                C v = p.grid[(f * p.coils + c) * p.Kprod + goff + n0];
+                v.x *= p.scale;
+                v.y *= p.scale;
+                v.x *= w;
+                v.y *= w;
+                const C t = cmulc(v, p.maps[(int64_t)c * p.Nprod + rr * p.N[0] + n0]);
+                acc.x += t.x;
+                acc.y += t.y;
+            }
+            dst[n0] = acc;
+        }
+    }
+}
+
 static int row_grid(int64_t nrows) {
     int64_t warps = nrows;
     int64_t blocks = (warps + 7) / 8;
@@ -83,15 +153,26 @@ template <typename R>
 cudaError_t launch_pad(const PadParams<R>& p, cudaStream_t s) {
     if (p.planes == 0 || p.Nprod == 0) return cudaSuccess;
     const int64_t nrows = (int64_t)p.N[1] * p.N[2] * p.planes;
-    pad_kernel<R><<<row_grid(nrows), 256, 0, s>>>(p);
+    if (p.maps) {
+        if (p.coils < 1) return cudaErrorInvalidValue;
+        pad_sense_kernel<R><<<row_grid(nrows), 256, 0, s>>>(p);
+    } else {
+        pad_kernel<R><<<row_grid(nrows), 256, 0, s>>>(p);
+    }
     return cudaGetLastError();
 }
 
 template <typename R>
 cudaError_t launch_crop(const CropParams<R>& p, cudaStream_t s) {
     if (p.planes == 0 || p.Nprod == 0) return cudaSuccess;
-    const int64_t nrows = (int64_t)p.N[1] * p.N[2] * p.planes;
-    crop_kernel<R><<<row_grid(nrows), 256, 0, s>>>(p);
+    if (p.maps) {
+        if (p.coils < 1 || p.planes % p.coils) return cudaErrorInvalidValue;
+        const int64_t nrows = (int64_t)p.N[1] * p.N[2] * (p.planes / p.coils);
+        crop_sense_kernel<R><<<row_grid(nrows), 256, 0, s>>>(p);
+    } else {
+        const int64_t nrows = (int64_t)p.N[1] * p.N[2] * p.planes;
+        crop_kernel<R><<<row_grid(nrows), 256, 0, s>>>(p);
+    }
     return cudaGetLastError();
 }
 

@@ -719,7 +719,7 @@ int run_spread_noalloc(gbn_plan* P, const void* y, void* grid, int coils, cudaSt
 }
 
 template <typename R>
-int run_forward(gbn_plan* P, const void* x, void* y, int coils, cudaStream_t s) {
+int run_forward(gbn_plan* P, const void* x, void* y, int coils, cudaStream_t s, const void* maps = nullptr) {
     int rc = ensure_buffers(P, coils);
     if (rc) return rc;
     if (!P->pad.p || !P->grid.p) return fail(GBN_ERR_NOMEM, "transform buffers missing");
@@ -737,6 +737,8 @@ int run_forward(gbn_plan* P, const void* x, void* y, int coils, cudaStream_t s) 
     pp.x = reinterpret_cast<const typename Cx<R>::T*>(x);
     pp.sn = reinterpret_cast<const R*>(P->sn.p);
     pp.out = reinterpret_cast<typename Cx<R>::T*>(P->pad.p);
+    pp.maps = reinterpret_cast<const typename Cx<R>::T*>(maps);
+    pp.coils = coils;
     GBN_CUDA(launch_pad<R>(pp, s), "pad launch");
     cufftHandle h;
     if ((rc = get_fft(P, P->F * coils, &h))) return rc;
@@ -745,7 +747,7 @@ int run_forward(gbn_plan* P, const void* x, void* y, int coils, cudaStream_t s) 
 }
 
 template <typename R>
-int run_adjoint(gbn_plan* P, const void* y, void* x, int coils, cudaStream_t s) {
+int run_adjoint(gbn_plan* P, const void* y, void* x, int coils, cudaStream_t s, const void* maps = nullptr) {
     // allocate first: the grid pointer handed to the spread must be the
     // buffer this call will use (it is null before the first call)
     int rc = ensure_buffers(P, coils);
@@ -771,6 +773,8 @@ int run_adjoint(gbn_plan* P, const void* y, void* x, int coils, cudaStream_t s) 
     cp.sn = reinterpret_cast<const R*>(P->sn.p);
     cp.scale = G.ortho ? (R)(G.adjoint_scale / std::sqrt((double)P->Kprod)) : (R)G.adjoint_scale;
     cp.x = reinterpret_cast<typename Cx<R>::T*>(x);
+    cp.maps = reinterpret_cast<const typename Cx<R>::T*>(maps);
+    cp.coils = coils;
     GBN_CUDA(launch_crop<R>(cp, s), "crop launch");
     return GBN_OK;
 }
@@ -1019,6 +1023,26 @@ int gbn_adjoint(gbn_plan* P, const void* y, void* x, int coils, void* stream) {
     DeviceGuard guard(P->device);
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
     return P->dbl ? run_adjoint<double>(P, y, x, coils, s) : run_adjoint<float>(P, y, x, coils, s);
+}
+
+int gbn_forward_sense(gbn_plan* P, const void* image, const void* maps, void* y, int coils, void* stream) {
+    int rc = check_call(P, image, y, coils);
+    if (rc) return rc;
+    if (!maps || !image) return fail(GBN_ERR_INVALID, "null image or coil maps");
+    std::lock_guard<std::mutex> lk(P->mu);
+    DeviceGuard guard(P->device);
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    return P->dbl ? run_forward<double>(P, image, y, coils, s, maps) : run_forward<float>(P, image, y, coils, s, maps);
+}
+
+int gbn_adjoint_sense(gbn_plan* P, const void* y, const void* maps, void* image, int coils, void* stream) {
+    int rc = check_call(P, y, image, coils);
+    if (rc) return rc;
+    if (!maps || !image) return fail(GBN_ERR_INVALID, "null image or coil maps");
+    std::lock_guard<std::mutex> lk(P->mu);
+    DeviceGuard guard(P->device);
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    return P->dbl ? run_adjoint<double>(P, y, image, coils, s, maps) : run_adjoint<float>(P, y, image, coils, s, maps);
 }
 
 int gbn_interp_forward(gbn_plan* P, const void* grid, void* y, int coils, void* stream) {

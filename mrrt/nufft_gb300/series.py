@@ -121,6 +121,26 @@ class NufftSeries(object):
         self.plan.adjoint(y, x, c)
         return x
 
+    # ------------------------------------------ coil sensitivities (fused)
+    def forward_sense(self, image, maps, y=None):
+        """One image per frame ``[F, *reversed(Nd)]`` and coil maps
+        ``[coils, *reversed(Nd)]`` -> frame-major samples of every coil; the
+        map multiply is fused into the deapodisation pass."""
+        c = maps.shape[0]
+        y = self.empty_samples(c) if y is None else y
+        self.plan.forward_sense(image, maps, y, c)
+        return y
+
+    def adjoint_sense(self, y, maps, image=None):
+        """Frame-major samples -> ``[F, *reversed(Nd)]``, the coil sum of
+        conj(maps) times each coil's adjoint fused into the crop pass."""
+        c = maps.shape[0]
+        if image is None:
+            image = torch.empty((self.n_frames,) + tuple(reversed(self.Nd)), dtype=self.ctype,
+                                device=self.device)
+        self.plan.adjoint_sense(y, maps, image, c)
+        return image
+
     # ------------------------------------------------------------ CUDA graphs
     def capture(self, coils=None, warmup=2):
         """Record forward and adjoint as CUDA graphs on static buffers
