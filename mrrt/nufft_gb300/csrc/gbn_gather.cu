@@ -281,7 +281,7 @@ static cudaError_t gather_specialised(const GatherParams<float>& p, cudaStream_t
     const int LS = p.ln.LS;
 #define GBN_G(JV, LV) \
     if (J == JV && LS == LV) return gather_launch<float, NDIM, false, JV, LV>(p, s);
-    GBN_G(6, 32) GBN_G(6, 8) GBN_G(6, 1) GBN_G(4, 32) GBN_G(4, 8) GBN_G(4, 1)
+    GBN_G(6, 32) GBN_G(6, 16) GBN_G(6, 8) GBN_G(6, 1) GBN_G(4, 32) GBN_G(4, 16) GBN_G(4, 8) GBN_G(4, 1)
 #undef GBN_G
     *done = false;
     return cudaSuccess;

@@ -1010,6 +1010,7 @@ static int check_call(gbn_plan* P, const void* a, const void* b, int coils) {
 int gbn_forward(gbn_plan* P, const void* x, void* y, int coils, void* stream) {
     int rc = check_call(P, x, y, coils);
     if (rc) return rc;
+    if (!x) return fail(GBN_ERR_INVALID, "null image");   // read even without samples
     std::lock_guard<std::mutex> lk(P->mu);
     DeviceGuard guard(P->device);
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
@@ -1019,6 +1020,7 @@ int gbn_forward(gbn_plan* P, const void* x, void* y, int coils, void* stream) {
 int gbn_adjoint(gbn_plan* P, const void* y, void* x, int coils, void* stream) {
     int rc = check_call(P, y, x, coils);
     if (rc) return rc;
+    if (!x) return fail(GBN_ERR_INVALID, "null image");   // written even without samples
     std::lock_guard<std::mutex> lk(P->mu);
     DeviceGuard guard(P->device);
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
@@ -1058,6 +1060,7 @@ int gbn_interp_forward(gbn_plan* P, const void* grid, void* y, int coils, void* 
 int gbn_interp_adjoint(gbn_plan* P, const void* y, void* grid, int coils, void* stream) {
     int rc = check_call(P, y, grid, coils);
     if (rc) return rc;
+    if (!grid) return fail(GBN_ERR_INVALID, "null grid");   // written even without samples
     std::lock_guard<std::mutex> lk(P->mu);
     DeviceGuard guard(P->device);
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
@@ -1068,6 +1071,7 @@ int gbn_interp_adjoint(gbn_plan* P, const void* y, void* grid, int coils, void* 
 int gbn_interp_adjoint_noalloc(gbn_plan* P, const void* y, void* grid, int coils, void* stream) {
     int rc = check_call(P, y, grid, coils);
     if (rc) return rc;
+    if (!grid) return fail(GBN_ERR_INVALID, "null grid");
     std::lock_guard<std::mutex> lk(P->mu);
     DeviceGuard guard(P->device);
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);

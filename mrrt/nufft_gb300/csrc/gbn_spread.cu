@@ -506,7 +506,7 @@ static cudaError_t spread_specialised(const SpreadParams<float>& p, cudaStream_t
     const int LS = p.ln.LS;
 #define GBN_S(JV, LV) \
     if (J == JV && LS == LV) return spread_launch<float, NDIM, false, JV, LV>(p, s);
-    GBN_S(6, 32) GBN_S(6, 8) GBN_S(6, 1) GBN_S(4, 32) GBN_S(4, 8) GBN_S(4, 1)
+    GBN_S(6, 32) GBN_S(6, 16) GBN_S(6, 8) GBN_S(6, 1) GBN_S(4, 32) GBN_S(4, 16) GBN_S(4, 8) GBN_S(4, 1)
 #undef GBN_S
     *done = false;
     return cudaSuccess;

@@ -304,3 +304,47 @@ def test_precomputed_coefficients_bitwise_equal_table_path(gpu_lib, ndim, K, J, 
           for P in plans]
     assert torch.equal(gs[0], gs[1])
 
+
+
+def test_outputs_written_without_samples_must_not_be_null(gpu_lib):
+    """With an empty trajectory the sample arrays may be NULL, but the image
+    (forward input, adjoint output) and the adjoint grid are still read or
+    written, so NULL there is an argument error, not a launch."""
+    import ctypes
+
+    from mrrt.nufft_gb300 import _lib
+    from mrrt.nufft_gb300._kernels import kernel_table
+    from mrrt.nufft_gb300._plan import GpuPlan
+
+    N, K, J, L = (16, 16), (32, 32), (6, 6), 512
+    h = [kernel_table(N[d], J[d], K[d], L, "real", np.float32) for d in range(2)]
+    P = GpuPlan(N, K, J, L, np.float32, h, None, np.ones(256, np.float32), np.zeros((0, 2), np.float32), None)
+    assert P.M_total == 0
+    for name in ("gbn_forward", "gbn_adjoint", "gbn_interp_adjoint", "gbn_interp_adjoint_noalloc"):
+        rc = getattr(P.lib, name)(P.handle, None, None, 1, None)
+        assert rc == _lib.GBN_ERR_INVALID, name
+
+
+@pytest.mark.parametrize("order,reps", [("F", 32), ("C", 48), ("F", 40)])
+def test_host_array_pipeline_matches_one_piece(gpu_lib, order, reps):
+    """Host numpy batches of 32 or more repetitions go through the chunked
+    copy/compute pipeline (chunks of 16, the last one shorter); the result
+    equals the one-piece device path."""
+    from mrrt.nufft_gb300 import NufftBase
+    from mrrt.nufft_gb300.trajectories import complex_image, radial_2d
+
+    Nd, Kd = (64, 48), (128, 96)
+    om = radial_2d(60, 128, golden=True)
+    kw = dict(Nd=Nd, omega=om, Jd=(6, 6), Kd=Kd, order=order, max_coils=reps)
+    Ah = NufftBase(on_gpu=False, **kw)
+    Ad = NufftBase(on_gpu=True, **kw)
+    x = np.stack([complex_image(Nd, seed=s) for s in range(reps)], axis=0 if order == "C" else -1)
+    if order == "F":
+        x = np.asfortranarray(x)
+    y = Ah.fft(x)
+    assert isinstance(y, np.ndarray) and y.shape == ((reps, Ah.M) if order == "C" else (Ah.M, reps))
+    yd = Ad.fft(x).cpu().numpy()
+    assert rel_l2(y, yd) < 1e-6
+    xa = Ah.adj(y)
+    assert xa.shape == x.shape
+    assert rel_l2(xa, Ad.adj(y).cpu().numpy()) < 1e-6
