@@ -135,6 +135,9 @@ class NufftBase(object):
         if order not in ("F", "C"):
             raise ValueError("order must be 'F' or 'C'")
         self.on_gpu = on_gpu
+        # the reference's attribute: the interpolation matrix format in
+        # sparse mode (mrrt/nufft/_nufft.py:319-323), None in table mode
+        self.__sparse_format = "CSC" if mode == "sparse" else None
         if np.isscalar(Nd):
             Nd = (Nd,)
         self.__Nd = _as_tuple(Nd, type=int)
@@ -224,6 +227,24 @@ class NufftBase(object):
             self._plan.set_weights(*self._weights)
 
     # ------------------------------------------------------------------ props
+    @property
+    def on_gpu(self):
+        """bool: results are returned as torch CUDA tensors (True) or numpy
+        arrays (False); the transforms always run on the GPU."""
+        return self.__on_gpu
+
+    @on_gpu.setter
+    def on_gpu(self, on_gpu):
+        if on_gpu in [True, False]:
+            self.__on_gpu = bool(on_gpu)
+        else:
+            raise ValueError("on_gpu must be True or False")
+
+    @property
+    def sparse_format(self):
+        """str: internal sparse matrix format (``'CSC'`` when ``mode=='sparse'``)."""
+        return self.__sparse_format
+
     @property
     def Nd(self):
         return self.__Nd

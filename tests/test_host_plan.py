@@ -114,3 +114,15 @@ def test_autotune_cache_round_trip(tmp_path):
         assert t[0] % 4 == 0 and t[1] % 4 == 0 and (t[0] // 4) * (t[1] // 4) <= 8
     for t in s3:
         assert t[0] % 4 == 0 and t[1] % 4 == 0 and (t[0] // 4) * (t[1] // 4) * t[2] <= 8
+
+
+def test_reference_attributes_on_gpu_and_sparse_format(host_nufft):
+    c = cases.radial_2d_128()
+    A = host_nufft(**c["kw"])
+    assert A.on_gpu is False and A.sparse_format is None
+    with pytest.raises(ValueError):
+        A.on_gpu = "yes"
+    A.on_gpu = True
+    assert A.on_gpu is True
+    kw = dict(c["kw"], mode="sparse")
+    assert host_nufft(**kw).sparse_format == "CSC"
