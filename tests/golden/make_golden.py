@@ -64,6 +64,7 @@ def main():
     np.savez_compressed(os.path.join(HERE, "tables.npz"), **tabs)
 
     make_sparse(ref)
+    make_kaiser(ref)
 
     # 4. exact NUDFT reference values
     d = {}
@@ -74,6 +75,43 @@ def main():
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))
+
+
+def make_kaiser(ref=None):
+    """The exported Kaiser-Bessel helpers on the parameter sets of the
+    reference's own tests (mrrt/nufft/tests/test_kaiser.py), the Beatty
+    kernel shape parameters, and kernel values at random points."""
+    ref = ref or load_reference()
+    import warnings
+
+    from mrrt.nufft import _kaiser_bessel as kb
+    from mrrt.nufft._kernels import BeattyKernel
+
+    out = {}
+    J, alpha = 8, 2.34 * 8
+    x = np.linspace(-(J + 1) / 2.0, (J + 1) / 2.0, 1001)
+    for m in (-4, 0, 2, 7):
+        with warnings.catch_warnings():
+            warnings.simplefilter("ignore")
+            out["kb_J8_m%d" % m] = kb.kaiser_bessel(x, J, alpha, m)
+    J, alpha, N = 5, 6.8, 2 ** 10
+    xx = np.arange(-N / 2.0, N / 2.0) / float(N) * (J + 3) / 2.0
+    du = 1 / float(N) / float(xx[1] - xx[0])
+    u = np.arange(-N / 2.0, N / 2.0) * du
+    for m in (-2, 0, 2, 7):
+        with warnings.catch_warnings():
+            warnings.simplefilter("ignore")
+            out["kbft_J5_m%d" % m] = kb.kaiser_bessel_ft(u, J, alpha, m, 1)
+    for d in (2, 3):
+        out["kbft_J6_d%d" % d] = kb.kaiser_bessel_ft(np.linspace(-1.5, 1.5, 301), 6, 2.34 * 6, 0, d)
+    for shape, grid, os_grid in (((6, 6), (256, 256), (512, 512)), ((4, 7), (64, 48), (96, 80)),
+                                 ((6, 6, 6), (128, 128, 128), (256, 256, 256))):
+        kern = BeattyKernel(shape=shape, grid_shape=grid, os_grid_shape=os_grid)
+        tag = "x".join(map(str, shape)) + "_" + "x".join(map(str, grid)) + "_" + "x".join(map(str, os_grid))
+        out["beatty_alpha_" + tag] = np.asarray(kern.alpha, dtype=np.float64)
+        pts = np.random.default_rng(3).uniform(-4, 4, 64)
+        out["beatty_k0_" + tag] = np.asarray(kern.kernels[0](pts))
+    np.savez_compressed(os.path.join(HERE, "kaiser.npz"), **out)
 
 
 def make_sparse(ref=None):
@@ -99,5 +137,7 @@ def make_sparse(ref=None):
 if __name__ == "__main__":
     if sys.argv[1:] == ["--sparse-only"]:
         make_sparse()
+    elif sys.argv[1:] == ["--kaiser-only"]:
+        make_kaiser()
     else:
         main()

@@ -60,19 +60,25 @@ def test_radial128_error_vs_exact_no_worse_than_reference(nb):
     assert err_gpu_a <= err_ref_a * 1.01, (err_gpu_a, err_ref_a)
 
 
+@pytest.mark.parametrize("order", ["F", "C"])
 @pytest.mark.parametrize("name", [n for n, _ in cases.small_cases()])
-def test_reference_test_geometries(nb, name):
+def test_reference_test_geometries(nb, name, order):
+    """The reference's test geometries (test_nufft.py:99-324) in both array
+    orders, single image and a 3-repetition batch, against its outputs."""
     g = cases.load("small_cases")
     c = dict(cases.small_cases())[name]
-    A = nb(**c["kw"])
+    A = nb(**dict(c["kw"], order=order))
     tol = tol_for(c["kw"]["precision"])
     y = A.fft(c["x"])
     assert rel_l2(y, g[name + "_y"]) < tol
     assert rel_l2(A.adj(y), g[name + "_xadj"]) < tol
-    reps = np.stack((c["x"],) * 3, axis=-1)
+    axis = 0 if order == "C" else -1
+    reps = np.stack((c["x"],) * 3, axis=axis)
     yr = A.fft(reps)
-    assert yr.shape == (A.M, 3)
-    assert rel_l2(yr, g[name + "_yreps"]) < tol
+    assert yr.shape == ((3, A.M) if order == "C" else (A.M, 3))
+    assert rel_l2(yr.T if order == "C" else yr, g[name + "_yreps"]) < tol
+    xr = A.adj(yr)
+    assert xr.shape == reps.shape
     # the reference tests' own tolerance against the exact NUDFT
     kw = c["kw"]
     yt = O.dtft(c["x"], kw["omega"], kw["Nd"], kw["n_shift"])
@@ -348,3 +354,17 @@ def test_host_array_pipeline_matches_one_piece(gpu_lib, order, reps):
     xa = Ah.adj(y)
     assert xa.shape == x.shape
     assert rel_l2(xa, Ad.adj(y).cpu().numpy()) < 1e-6
+
+
+def test_exported_dtft_matches_reference(gpu_lib):
+    """mrrt.nufft_gb300.dtft / dtft_adj (FP64 direct NUDFT on the GPU)
+    against the reference's dtft / dtft_adj (mrrt/nufft/_dtft.py)."""
+    from mrrt.nufft_gb300 import dtft, dtft_adj
+
+    g = cases.load("dtft")
+    c = cases.dtft_case()
+    y = dtft(c["x"], c["omega"], shape=c["Nd"], n_shift=c["n_shift"])
+    assert rel_l2(y, g["dtft_y"]) < 1e-12
+    xa = dtft_adj(c["y"], c["omega"], shape=c["Nd"], n_shift=c["n_shift"])
+    assert rel_l2(xa, g["dtft_xadj"]) < 1e-12
+

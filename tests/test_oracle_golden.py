@@ -94,3 +94,36 @@ def test_oracle_interp_bit_identical_to_reference_c():
     g_ref = interp2_table_adj(np.asfortranarray(fm), h[0], h[1], (6, 6), 512, tm, K)
     g_or = O.interp_adjoint(fm, h, (6, 6), 512, tm, K)
     assert rel_l2(g_or, g_ref) < 1e-6
+
+
+def test_exported_kaiser_bessel_helpers_match_reference():
+    """kaiser_bessel, kaiser_bessel_ft and BeattyKernel (exported like the
+    reference's, mrrt/nufft/__init__.py) against values the reference
+    computed on the parameter sets of its own tests."""
+    import warnings
+
+    from mrrt.nufft_gb300 import BeattyKernel, kaiser_bessel, kaiser_bessel_ft
+
+    g = cases.load("kaiser")
+    J, alpha = 8, 2.34 * 8
+    x = np.linspace(-(J + 1) / 2.0, (J + 1) / 2.0, 1001)
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        for m in (-4, 0, 2, 7):
+            np.testing.assert_allclose(kaiser_bessel(x, J, alpha, m), g["kb_J8_m%d" % m], rtol=1e-12, atol=1e-15)
+        J, alpha, N = 5, 6.8, 2 ** 10
+        xx = np.arange(-N / 2.0, N / 2.0) / float(N) * (J + 3) / 2.0
+        u = np.arange(-N / 2.0, N / 2.0) * (1 / float(N) / float(xx[1] - xx[0]))
+        for m in (-2, 0, 2, 7):
+            np.testing.assert_allclose(kaiser_bessel_ft(u, J, alpha, m, 1), g["kbft_J5_m%d" % m],
+                                       rtol=1e-10, atol=1e-14)
+    for d in (2, 3):
+        np.testing.assert_allclose(kaiser_bessel_ft(np.linspace(-1.5, 1.5, 301), 6, 2.34 * 6, 0, d),
+                                   g["kbft_J6_d%d" % d], rtol=1e-10, atol=1e-14)
+    pts = np.random.default_rng(3).uniform(-4, 4, 64)
+    for shape, grid, os_grid in (((6, 6), (256, 256), (512, 512)), ((4, 7), (64, 48), (96, 80)),
+                                 ((6, 6, 6), (128, 128, 128), (256, 256, 256))):
+        kern = BeattyKernel(shape=shape, grid_shape=grid, os_grid_shape=os_grid)
+        tag = "x".join(map(str, shape)) + "_" + "x".join(map(str, grid)) + "_" + "x".join(map(str, os_grid))
+        np.testing.assert_allclose(np.asarray(kern.alpha, dtype=np.float64), g["beatty_alpha_" + tag], rtol=1e-14)
+        np.testing.assert_allclose(kern.kernels[0](pts), g["beatty_k0_" + tag], rtol=1e-12, atol=1e-15)
