@@ -482,7 +482,10 @@ int build_lists(gbn_plan* P, const R* tm, const R* phase) {
     for (int64_t b = 0; b < nbins_s; ++b) {
         const int f = (int)(b / nts), tile = (int)(b % nts);
         const int64_t s0 = scount[b], sn = scount[b + 1] - s0;
-        const int parts = (int)std::max<int64_t>(1, (sn + SPREAD_CHUNK - 1) / SPREAD_CHUNK);
+        // 3-D items are larger: a sample enters about 8 spread tiles, so the
+        // tiles are lighter and the per-item overhead weighs more (measured)
+        const int SCH = G.ndim == 3 ? 2 * SPREAD_CHUNK : SPREAD_CHUNK;
+        const int parts = (int)std::max<int64_t>(1, (sn + SCH - 1) / SCH);
         if (parts == 1) {
             si.push_back({make_int4(f, tile, (int)s0, (int)sn), make_int2(-1, 1)});
         } else {

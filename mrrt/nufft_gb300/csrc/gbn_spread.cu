@@ -178,7 +178,9 @@ spread_kernel(const SpreadParams<R> p) {
 
     // zero padding of the coefficient rows: written once, the J coefficient
     // slots of each row are overwritten per chunk
-    for (int q = tid; q < CH * SL::PSTR; q += blockDim.x) cp[q] = cmake<R>((R)0, (R)0);
+    // (an empty tile -- no entry touches it -- needs no rows: it only writes zeros)
+    if (count > 0)
+        for (int q = tid; q < CH * SL::PSTR; q += blockDim.x) cp[q] = cmake<R>((R)0, (R)0);
     const int Jsum = Jx + (NDIM > 1 ? Jy : 0) + (NDIM > 2 ? Jz : 0);
 
     // Copy-in assignment: each thread owns up to two entries of a chunk and
@@ -336,7 +338,8 @@ spread_kernel(const SpreadParams<R> p) {
     C myph = cmake<R>((R)1, (R)0);
     const int slot_id = part.x;
     const bool direct = slot_id < 0;
-    if (direct && p.apply_pb && lane < NB) {
+    // zeros need no phase: an empty tile skips the per-cell sincos
+    if (direct && p.apply_pb && lane < NB && count > 0) {
         const int k0 = lane % B0, k1 = (lane / B0) % B1, k2 = lane / (B0 * B1);
         int k[3] = {org[0] + bo0 + k0, org[1] + bo1 + k1, org[2] + bo2 + k2};
         bool in = bo0 + k0 < ext[0];
@@ -351,7 +354,7 @@ spread_kernel(const SpreadParams<R> p) {
     for (int q = 0; q < NB; q += 2) {
         const int k0 = q % B0, k1 = (q / B0) % B1, k2 = q / (B0 * B1);
         C ph0 = cmake<R>((R)1, (R)0), ph1 = cmake<R>((R)1, (R)0);
-        if (direct && p.apply_pb) {
+        if (direct && p.apply_pb && count > 0) {
             ph0.x = __shfl_sync(0xffffffffu, myph.x, q);
             ph0.y = __shfl_sync(0xffffffffu, myph.y, q);
             ph1.x = __shfl_sync(0xffffffffu, myph.x, q + 1);
@@ -365,7 +368,7 @@ spread_kernel(const SpreadParams<R> p) {
         if (slot != 0 || coil >= nc) continue;
         C v0 = acc[q], v1 = acc[q + 1];
         if (direct) {
-            if (p.apply_pb) {
+            if (p.apply_pb && count > 0) {
                 v0 = cmulc(v0, ph0);
                 v1 = cmulc(v1, ph1);
             }
