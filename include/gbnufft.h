@@ -183,9 +183,10 @@ int gbn_plan_set_dtables(gbn_plan* plan, const void* const* dtab);
 
 /* Gradient of a real loss with respect to the sample coordinates tm
  * (single-frame plans, real phasing).
- *   grid : [coils][K...] the forward's oversampled grid before phase_before,
- *          i.e. the FFT output a gbn_forward call leaves in the buffer that
- *          gbn_forward_grid returns (callers copy it if they need it later).
+ *   grid : the forward's oversampled grid before phase_before, i.e. the FFT
+ *          output a gbn_forward call with the same coil count leaves in the
+ *          buffer that gbn_forward_grid returns (callers copy it if they need
+ *          it later), in that buffer's layout.
  *   gy   : [coils][M] dL/dy in torch's convention (dL/dRe + i dL/dIm).
  *   phase_shift : host [ndim], d(sample phase)/d(tm_d) divided by i, i.e.
  *          (n_shift_d - n_mid_d) * 2 pi / Kd[d] for phase_after.
@@ -195,7 +196,10 @@ int gbn_grad_tm(gbn_plan* plan, const void* grid, const void* gy,
                 const double* phase_shift, void* gtm, int coils, void* stream);
 
 /* Device pointer of the plan's forward grid buffer (valid until the next
- * call on the plan).                                                         */
+ * call on the plan).  Its layout is the transform's own: [coils][K...] for
+ * 1-D and 3-D plans, [K1][coils][K0] for 2-D plans (row k1 of every coil
+ * plane together, so the FFT's row pass skips the zero-padded rows).  The
+ * interpolation-only entry points keep the [planes][K...] layout.           */
 int gbn_forward_grid(gbn_plan* plan, void** grid);
 
 /* Exact direct NUDFT in double precision on the GPU (the reference's

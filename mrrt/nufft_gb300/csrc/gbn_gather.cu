@@ -79,7 +79,7 @@ gather_kernel(const GatherParams<R> p) {
 
     // ---- stage tile + halo for nc coils: thread per cell, coils in batches
     // of four independent loads ----------------------------------------------
-    const C* gb = p.grid + ((int64_t)f * p.coils + c0) * g.Kprod;
+    const C* gb = p.grid + ((int64_t)f * p.coils + c0) * g.gsp;
     for (int cell = threadIdx.x; cell < Rtot; cell += blockDim.x) {
         int r[3];
         int rem = cell;
@@ -88,13 +88,9 @@ gather_kernel(const GatherParams<R> p) {
         r[1] = rem % Rd[1];
         r[2] = rem / Rd[1];
         int k[3] = {0, 0, 0};
-        int64_t off = 0, stride = 1;
 #pragma unroll
-        for (int d = 0; d < NDIM; ++d) {
-            k[d] = wrapk(org[d] + r[d], g.K[d]);
-            off += (int64_t)k[d] * stride;
-            stride *= g.K[d];
-        }
+        for (int d = 0; d < NDIM; ++d) k[d] = wrapk(org[d] + r[d], g.K[d]);
+        const int64_t off = k[0] + (int64_t)k[1] * g.gs1 + (int64_t)k[2] * g.gs2;
         C ph = cmake<R>((R)1, (R)0);
         if (p.apply_pb) ph = phase_before(g, k);
         const int dst = cell * LSP;
@@ -103,7 +99,7 @@ gather_kernel(const GatherParams<R> p) {
             C v[4];
 #pragma unroll
             for (int u = 0; u < 4; ++u)
-                if (c + u < nc) v[u] = src[(int64_t)(c + u) * g.Kprod];
+                if (c + u < nc) v[u] = src[(int64_t)(c + u) * g.gsp];
 #pragma unroll
             for (int u = 0; u < 4; ++u) {
                 if (c + u < nc) {

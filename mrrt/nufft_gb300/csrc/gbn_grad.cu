@@ -54,7 +54,7 @@ __global__ void __launch_bounds__(128) grad_kernel(const GradParams<R> p) {
     const C ph = p.ph ? p.ph[m] : cmake<R>((R)1, (R)0);
     R out[3] = {0, 0, 0};
     for (int cc = 0; cc < p.coils; ++cc) {
-        const C* gb = p.grid + (int64_t)cc * g.Kprod;
+        const C* gb = p.grid + (int64_t)cc * g.gsp;
         C G = cmake<R>(0, 0), D[3] = {cmake<R>(0, 0), cmake<R>(0, 0), cmake<R>(0, 0)};
 #pragma unroll 1
         for (int j2 = 0; j2 < (NDIM > 2 ? JMAX : 1); ++j2) {
@@ -70,7 +70,7 @@ __global__ void __launch_bounds__(128) grad_kernel(const GradParams<R> p) {
                     k[0] = wrapk(kf[0] + j0, g.K[0]);
                     if (NDIM > 1) k[1] = wrapk(kf[NDIM > 1 ? 1 : 0] + j1, g.K[1]);
                     if (NDIM > 2) k[2] = wrapk(kf[NDIM > 2 ? 2 : 0] + j2, g.K[2]);
-                    const int64_t off = k[0] + (int64_t)g.K[0] * (k[1] + (int64_t)g.K[1] * k[2]);
+                    const int64_t off = k[0] + (int64_t)k[1] * g.gs1 + (int64_t)k[2] * g.gs2;
                     C v = gb[off];
                     if (p.apply_pb) v = cmul(v, phase_before(g, k));
                     v.x /= p.grid_scale;

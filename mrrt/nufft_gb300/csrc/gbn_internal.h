@@ -35,6 +35,12 @@ struct Geom {
     const R* hr[3];          // device tables (shifted past their zero padding)
     const R* hi[3];          // imaginary tables, nullptr for a real kernel
     int64_t Kprod, Nprod;
+    // Grid layout: cell (k0, k1, k2) of plane pl (= frame * coils + coil) at
+    // pl * gsp + k0 + k1 * gs1 + k2 * gs2.  Plane-major ([planes][K...]:
+    // gsp = Kprod, gs1 = K0, gs2 = K0 K1) or, for the 2-D transform's own
+    // grid, row-interleaved ([K1][planes][K0]: gsp = K0, gs1 = planes K0),
+    // the layout its pruned FFT passes need.
+    int64_t gsp, gs1, gs2;
     R pbc[3];                // phase_before coefficient per memory axis
     int pbo[3];              // summation order of the per-axis phases
 };
@@ -133,6 +139,7 @@ struct PadParams {
     int ndim;
     int N[3], K[3];
     int64_t Nprod, Kprod;
+    int64_t gsp, gs1, gs2;          // layout of the padded grid (see Geom)
     int planes;
     const typename Cx<R>::T* x;
     const R* sn;
@@ -148,6 +155,7 @@ struct CropParams {
     int ndim;
     int N[3], K[3];
     int64_t Nprod, Kprod;
+    int64_t gsp, gs1, gs2;          // layout of the grid read (see Geom)
     int planes;
     const typename Cx<R>::T* grid;
     const R* sn;

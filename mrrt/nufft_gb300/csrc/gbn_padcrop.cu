@@ -34,7 +34,7 @@ __global__ void __launch_bounds__(256) pad_kernel(const PadParams<R> p) {
         const int n2 = (int)(rr / p.N[1]);
         const C* src = p.x + pl * p.Nprod + rr * p.N[0];
         const R* s = p.sn + rr * p.N[0];
-        C* dst = p.out + pl * p.Kprod + ((int64_t)n2 * p.K[1] + n1) * p.K[0];
+        C* dst = p.out + pl * p.gsp + (int64_t)n1 * p.gs1 + (int64_t)n2 * p.gs2;
         for (int n0 = lane; n0 < p.N[0]; n0 += 32) {
             C v = src[n0];
             const R w = s[n0];
@@ -58,7 +58,7 @@ __global__ void __launch_bounds__(256) crop_kernel(const CropParams<R> p) {
         const int64_t rr = row - pl * rows_per_plane;
         const int n1 = (int)(rr % p.N[1]);
         const int n2 = (int)(rr / p.N[1]);
-        const C* src = p.grid + pl * p.Kprod + ((int64_t)n2 * p.K[1] + n1) * p.K[0];
+        const C* src = p.grid + pl * p.gsp + (int64_t)n1 * p.gs1 + (int64_t)n2 * p.gs2;
         const R* s = p.sn + rr * p.N[0];
         C* dst = p.x + pl * p.Nprod + rr * p.N[0];
         for (int n0 = lane; n0 < p.N[0]; n0 += 32) {
@@ -93,7 +93,7 @@ __global__ void __launch_bounds__(256) pad_sense_kernel(const PadParams<R> p) {
         const C* src = p.x + f * p.Nprod + rr * p.N[0];
         const C* mp = p.maps + c * p.Nprod + rr * p.N[0];
         const R* s = p.sn + rr * p.N[0];
-        C* dst = p.out + pl * p.Kprod + ((int64_t)n2 * p.K[1] + n1) * p.K[0];
+        C* dst = p.out + pl * p.gsp + (int64_t)n1 * p.gs1 + (int64_t)n2 * p.gs2;
         for (int n0 = lane; n0 < p.N[0]; n0 += 32) {
             C v = cmul(src[n0], mp[n0]);
             const R w = s[n0];
@@ -120,14 +120,14 @@ __global__ void __launch_bounds__(256) crop_sense_kernel(const CropParams<R> p) 
         const int64_t rr = row - f * rows_per_plane;
         const int n1 = (int)(rr % p.N[1]);
         const int n2 = (int)(rr / p.N[1]);
-        const int64_t goff = ((int64_t)n2 * p.K[1] + n1) * p.K[0];
+        const int64_t goff = (int64_t)n1 * p.gs1 + (int64_t)n2 * p.gs2;
         const R* s = p.sn + rr * p.N[0];
         C* dst = p.x + f * p.Nprod + rr * p.N[0];
         for (int n0 = lane; n0 < p.N[0]; n0 += 32) {
             const R w = s[n0];
             C acc = cmake<R>((R)0, (R)0);
             for (int c = 0; c < p.coils; ++c) {
-                C v = p.grid[(f * p.coils + c) * p.Kprod + goff + n0];
+                C v = p.grid[(f * p.coils + c) * p.gsp + goff + n0];
                 v.x *= p.scale;
                 v.y *= p.scale;
                 v.x *= w;

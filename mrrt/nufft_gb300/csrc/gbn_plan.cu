@@ -114,7 +114,8 @@ struct DevBuf {
 
 struct FftEntry {
     int planes;
-    cufftHandle h;
+    cufftHandle h;        // full transform (1-D, 3-D)
+    cufftHandle hx, hy;   // 2-D pruned passes: rows holding data, then all columns
 };
 
 constexpr int GATHER_CHUNK = 512;   // samples per gather work item
@@ -151,13 +152,19 @@ struct gbn_plan {
     int n_gitems = 0, n_sitems = 0, n_rtiles = 0, n_slots = 0;
     int64_t glen = 0, slen = 0;
     DevBuf pad, grid, scratch;
+    DevBuf mid;           // 2-D: output of the forward's row pass (rows >= N1 stay zero)
+    int64_t mid_clean = 0;     // rows of K0 cells from which mid is known to be zero
     int cap_planes = 0;        // planes the pad/grid buffers hold
     int64_t scratch_cap = 0;   // complex elements
     std::vector<FftEntry> ffts;
     std::mutex mu;
 
     ~gbn_plan() {
-        for (auto& f : ffts) cufftDestroy(f.h);
+        for (auto& f : ffts) {
+            if (f.h) cufftDestroy(f.h);
+            if (f.hx) cufftDestroy(f.hx);
+            if (f.hy) cufftDestroy(f.hy);
+        }
     }
 };
 
@@ -208,7 +215,31 @@ Geom<R> make_geom(const gbn_plan* P, bool spread) {
     g.L = G.L;
     g.Kprod = P->Kprod;
     g.Nprod = P->Nprod;
+    // plane-major layout (the C ABI's grids); transform-internal grids of
+    // 2-D plans are re-strided by internal_layout
+    g.gsp = P->Kprod;
+    g.gs1 = g.K[0];
+    g.gs2 = (int64_t)g.K[0] * g.K[1];
     return g;
+}
+
+// The 2-D transform keeps its grids row-interleaved, [K1][planes][K0]: row
+// r of every plane is one contiguous block, so the row FFT pass runs over the
+// first N1 * planes rows only (the others hold zero padding on the way in and
+// are cropped away on the way out) and the column pass is one strided batch.
+bool pruned_2d(const gbn_plan* P) { return P->geom.ndim == 2; }
+
+template <typename T>
+void internal_layout(const gbn_plan* P, int planes, T& g) {
+    if (pruned_2d(P)) {
+        g.gsp = P->geom.Kd[0];
+        g.gs1 = (int64_t)planes * P->geom.Kd[0];
+        g.gs2 = 0;
+    } else {
+        g.gsp = P->Kprod;
+        g.gs1 = P->geom.Kd[0];
+        g.gs2 = P->geom.ndim > 2 ? (int64_t)P->geom.Kd[0] * P->geom.Kd[1] : 0;
+    }
 }
 
 // Sample-list buffer layout: window starts (spread list only), sample
@@ -558,26 +589,49 @@ int ensure_buffers(gbn_plan* P, int coils) {
         if (e != cudaSuccess) return cuda_fail(e, "pad buffer clear");
         e = P->grid.alloc(bytes);
         if (e != cudaSuccess) return fail(GBN_ERR_NOMEM, "grid buffer allocation failed");
+        if (pruned_2d(P)) {
+            e = P->mid.alloc(bytes);
+            if (e != cudaSuccess) return fail(GBN_ERR_NOMEM, "row-pass buffer allocation failed");
+            e = cudaMemset(P->mid.p, 0, bytes);
+            if (e != cudaSuccess) return cuda_fail(e, "row-pass buffer clear");
+            P->mid_clean = 0;
+        }
         P->cap_planes = planes;
     }
     return ensure_scratch(P, coils);
 }
 
-int get_fft(gbn_plan* P, int planes, cufftHandle* out) {
+int get_fft(gbn_plan* P, int planes, FftEntry** out) {
     for (auto& f : P->ffts)
         if (f.planes == planes) {
-            *out = f.h;
+            *out = &f;
             return GBN_OK;
         }
     const gbn_geometry& G = P->geom;
-    int n[3];
-    for (int d = 0; d < G.ndim; ++d) n[d] = G.Kd[G.ndim - 1 - d];
-    cufftHandle h;
-    cufftResult r = cufftPlanMany(&h, G.ndim, n, nullptr, 1, (int)P->Kprod, nullptr, 1, (int)P->Kprod,
-                                  P->dbl ? CUFFT_Z2Z : CUFFT_C2C, planes);
-    if (r != CUFFT_SUCCESS) return cufft_fail(r, "cufftPlanMany");
-    P->ffts.push_back({planes, h});
-    *out = h;
+    const cufftType type = P->dbl ? CUFFT_Z2Z : CUFFT_C2C;
+    FftEntry f{planes, 0, 0, 0};
+    cufftResult r;
+    if (pruned_2d(P)) {
+        const int K0 = G.Kd[0], K1 = G.Kd[1], N1 = G.Nd[1];
+        int nx[1] = {K0}, ny[1] = {K1};
+        // rows k1 < N1 of every plane: N1 * planes contiguous rows of K0
+        r = cufftPlanMany(&f.hx, 1, nx, nullptr, 1, K0, nullptr, 1, K0, type, N1 * planes);
+        if (r != CUFFT_SUCCESS) return cufft_fail(r, "cufftPlanMany (rows)");
+        // every column (plane, k0): stride planes * K0 between k1, adjacent columns
+        int emb[1] = {K1};
+        r = cufftPlanMany(&f.hy, 1, ny, emb, planes * K0, 1, emb, planes * K0, 1, type, planes * K0);
+        if (r != CUFFT_SUCCESS) {
+            cufftDestroy(f.hx);
+            return cufft_fail(r, "cufftPlanMany (columns)");
+        }
+    } else {
+        int n[3];
+        for (int d = 0; d < G.ndim; ++d) n[d] = G.Kd[G.ndim - 1 - d];
+        r = cufftPlanMany(&f.h, G.ndim, n, nullptr, 1, (int)P->Kprod, nullptr, 1, (int)P->Kprod, type, planes);
+        if (r != CUFFT_SUCCESS) return cufft_fail(r, "cufftPlanMany");
+    }
+    P->ffts.push_back(f);
+    *out = &P->ffts.back();
     return GBN_OK;
 }
 
@@ -590,6 +644,48 @@ int exec_fft(gbn_plan* P, cufftHandle h, void* in, void* out, int dir, cudaStrea
         r = cufftExecC2C(h, (cufftComplex*)in, (cufftComplex*)out, dir);
     if (r != CUFFT_SUCCESS) return cufft_fail(r, "cufftExec");
     return GBN_OK;
+}
+
+// Forward Kd-point FFT of the padded planes into the grid.  2-D: the row
+// pass only over the N1 rows that hold data (pad -> mid), then the column
+// pass over every column (mid -> grid).
+int fft_forward(gbn_plan* P, int planes, cudaStream_t s) {
+    FftEntry* f = nullptr;
+    int rc = get_fft(P, planes, &f);
+    if (rc) return rc;
+    if (pruned_2d(P)) {
+        // The column pass reads rows [N1 * planes, K1 * planes) of mid as
+        // zero.  A call with more planes wrote rows below N1 * cap_planes, so
+        // rows in [N1 * planes, mid_clean) are cleared first.  A stream being
+        // captured into a graph clears up to N1 * cap_planes on every replay,
+        // since eager calls between replays may write there.
+        const int64_t row = (int64_t)P->geom.Kd[0] * 2 * P->rsize;
+        const int64_t lo = (int64_t)P->geom.Nd[1] * planes;
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        GBN_CUDA(cudaStreamIsCapturing(s, &cs), "capture status");
+        const bool capturing = cs != cudaStreamCaptureStatusNone;
+        const int64_t hi = capturing ? (int64_t)P->geom.Nd[1] * P->cap_planes : P->mid_clean;
+        if (hi > lo)
+            GBN_CUDA(cudaMemsetAsync(static_cast<char*>(P->mid.p) + lo * row, 0, (size_t)((hi - lo) * row), s),
+                     "row-pass buffer clear");
+        P->mid_clean = capturing ? std::max(P->mid_clean, lo) : lo;
+        if ((rc = exec_fft(P, f->hx, P->pad.p, P->mid.p, CUFFT_FORWARD, s))) return rc;
+        return exec_fft(P, f->hy, P->mid.p, P->grid.p, CUFFT_FORWARD, s);
+    }
+    return exec_fft(P, f->h, P->pad.p, P->grid.p, CUFFT_FORWARD, s);
+}
+
+// Inverse FFT of the grid in place.  2-D: every column, then only the N1 rows
+// the crop reads.
+int fft_inverse(gbn_plan* P, int planes, cudaStream_t s) {
+    FftEntry* f = nullptr;
+    int rc = get_fft(P, planes, &f);
+    if (rc) return rc;
+    if (pruned_2d(P)) {
+        if ((rc = exec_fft(P, f->hy, P->grid.p, P->grid.p, CUFFT_INVERSE, s))) return rc;
+        return exec_fft(P, f->hx, P->grid.p, P->grid.p, CUFFT_INVERSE, s);
+    }
+    return exec_fft(P, f->h, P->grid.p, P->grid.p, CUFFT_INVERSE, s);
 }
 
 // Coil lanes for a call: as many as the coil count asks for, halved until
@@ -617,6 +713,7 @@ int run_gather(gbn_plan* P, const void* grid, void* y, int coils, bool phases, c
     p.nitems = P->n_gitems;
     p.coils = coils;
     p.foff = reinterpret_cast<const int64_t*>(P->dfoff.p);
+    if (phases) internal_layout(P, P->F * coils, p.g);   // the transform's own grid
     p.grid = reinterpret_cast<const C*>(grid);
     p.y = reinterpret_cast<C*>(y);
     p.apply_pb = phases && P->geom.phasing == GBN_PHASING_REAL;
@@ -641,6 +738,7 @@ int run_spread(gbn_plan* P, const void* y, void* grid, int coils, bool phases, c
     p.nitems = P->n_sitems;
     p.coils = coils;
     p.foff = reinterpret_cast<const int64_t*>(P->dfoff.p);
+    if (phases) internal_layout(P, P->F * coils, p.g);   // the transform's own grid
     p.y = reinterpret_cast<const C*>(y);
     p.grid = reinterpret_cast<C*>(grid);
     p.scratch = reinterpret_cast<C*>(P->scratch.p);
@@ -743,10 +841,9 @@ int run_forward(gbn_plan* P, const void* x, void* y, int coils, cudaStream_t s, 
     pp.out = reinterpret_cast<typename Cx<R>::T*>(P->pad.p);
     pp.maps = reinterpret_cast<const typename Cx<R>::T*>(maps);
     pp.coils = coils;
+    internal_layout(P, P->F * coils, pp);
     GBN_CUDA(launch_pad<R>(pp, s), "pad launch");
-    cufftHandle h;
-    if ((rc = get_fft(P, P->F * coils, &h))) return rc;
-    if ((rc = exec_fft(P, h, P->pad.p, P->grid.p, CUFFT_FORWARD, s))) return rc;
+    if ((rc = fft_forward(P, P->F * coils, s))) return rc;
     return run_gather<R>(P, P->grid.p, y, coils, true, s);
 }
 
@@ -759,9 +856,7 @@ int run_adjoint(gbn_plan* P, const void* y, void* x, int coils, cudaStream_t s, 
     if (!P->grid.p) return fail(GBN_ERR_NOMEM, "grid buffer missing");
     rc = run_spread<R>(P, y, P->grid.p, coils, true, s);
     if (rc) return rc;
-    cufftHandle h;
-    if ((rc = get_fft(P, P->F * coils, &h))) return rc;
-    if ((rc = exec_fft(P, h, P->grid.p, P->grid.p, CUFFT_INVERSE, s))) return rc;
+    if ((rc = fft_inverse(P, P->F * coils, s))) return rc;
     const gbn_geometry& G = P->geom;
     CropParams<R> cp;
     std::memset(&cp, 0, sizeof(cp));
@@ -779,6 +874,7 @@ int run_adjoint(gbn_plan* P, const void* y, void* x, int coils, cudaStream_t s, 
     cp.x = reinterpret_cast<typename Cx<R>::T*>(x);
     cp.maps = reinterpret_cast<const typename Cx<R>::T*>(maps);
     cp.coils = coils;
+    internal_layout(P, P->F * coils, cp);
     GBN_CUDA(launch_crop<R>(cp, s), "crop launch");
     return GBN_OK;
 }
@@ -912,6 +1008,7 @@ int run_grad(gbn_plan* P, const void* grid, const void* gy, const double* shift,
     GradParams<R> p;
     std::memset(&p, 0, sizeof(p));
     p.g = make_geom<R>(P, false);
+    internal_layout(P, P->F * coils, p.g);   // the grid a forward call with these coils left
     const SampleList<R> L = make_list<R>(P, P->glist, P->glen, false);
     const R* db = reinterpret_cast<const R*>(P->dtables.p);
     size_t off = 0;
@@ -1188,7 +1285,7 @@ int gbn_plan_stats(const gbn_plan* P, int64_t* o) {
     o[3] = P->glen;
     o[4] = P->slen;
     o[5] = (int64_t)P->ntiles_s * P->F;
-    o[6] = (int64_t)(P->tables.bytes + P->weights.bytes + P->gcoef.bytes + P->scoef.bytes + P->sn.bytes + P->glist.bytes + P->slist.bytes + P->pad.bytes +
+    o[6] = (int64_t)(P->tables.bytes + P->weights.bytes + P->gcoef.bytes + P->scoef.bytes + P->mid.bytes + P->sn.bytes + P->glist.bytes + P->slist.bytes + P->pad.bytes +
                      P->grid.bytes + P->scratch.bytes);
     o[7] = P->M_total;
     return GBN_OK;

@@ -349,7 +349,8 @@ spread_kernel(const SpreadParams<R> p) {
     }
     // cells are written in adjacent pairs: one 16-byte store when both are
     // inside the grid and the address is aligned (single precision, even K0)
-    const bool vec_ok = sizeof(R) == 4 && (g.K[0] % 2) == 0;
+    const bool vec_ok = sizeof(R) == 4 && (g.K[0] % 2) == 0 && (g.gsp % 2) == 0 && (g.gs1 % 2) == 0 &&
+                        (g.gs2 % 2) == 0;
 #pragma unroll
     for (int q = 0; q < NB; q += 2) {
         const int k0 = q % B0, k1 = (q / B0) % B1, k2 = q / (B0 * B1);
@@ -372,9 +373,9 @@ spread_kernel(const SpreadParams<R> p) {
                 v0 = cmulc(v0, ph0);
                 v1 = cmulc(v1, ph1);
             }
-            const int64_t off = (int64_t)(org[0] + l0) +
-                                (int64_t)g.K[0] * ((int64_t)(org[1] + l1) + (int64_t)g.K[1] * (org[2] + l2));
-            C* dst = p.grid + ((int64_t)f * p.coils + c0 + coil) * g.Kprod + off;
+            const int64_t off = (int64_t)(org[0] + l0) + (int64_t)(org[1] + l1) * g.gs1 +
+                                (int64_t)(org[2] + l2) * g.gs2;
+            C* dst = p.grid + ((int64_t)f * p.coils + c0 + coil) * g.gsp + off;
             if (in0 && in1 && vec_ok) {
                 store_pair(dst, v0, v1);
             } else {
@@ -446,15 +447,11 @@ __global__ void __launch_bounds__(256) reduce_kernel(const ReduceParams<R> p, co
         acc.y += v.y;
     }
     int k[3] = {0, 0, 0};
-    int64_t off = 0, stride = 1;
 #pragma unroll
-    for (int d = 0; d < NDIM; ++d) {
-        k[d] = org[d] + r[d];
-        off += (int64_t)k[d] * stride;
-        stride *= g.K[d];
-    }
+    for (int d = 0; d < NDIM; ++d) k[d] = org[d] + r[d];
+    const int64_t off = k[0] + (int64_t)k[1] * g.gs1 + (int64_t)k[2] * g.gs2;
     if (p.apply_pb) acc = cmulc(acc, phase_before(g, k));
-    p.grid[((int64_t)f * p.coils + c0 + c) * g.Kprod + off] = acc;
+    p.grid[((int64_t)f * p.coils + c0 + c) * g.gsp + off] = acc;
 }
 
 template <typename R>

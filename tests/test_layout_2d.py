@@ -1,0 +1,97 @@
+"""2-D plans keep their transform grid row-interleaved, [K1][planes][K0], so
+the FFT's row pass runs over the N1 rows that hold data only.  The column
+pass then reads the other rows of its input as zero.  These tests change the
+coil count between calls (a call with more coil planes writes rows that a call
+with fewer reads as padding) and replay a CUDA graph captured with few coils
+after an eager call with more; every result must equal single-coil calls on a
+fresh operator.  A non-square image and grid catch swapped axes."""
+import numpy as np
+import pytest
+import torch
+
+from tests.conftest import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+ND, KD, COILS = (40, 48), (80, 96), 6
+
+
+def _operator(max_coils):
+    from mrrt.nufft_gb300 import NufftBase
+    from mrrt.nufft_gb300.trajectories import radial_2d
+
+    return NufftBase(ND, radial_2d(21, 96, golden=True), Jd=(6, 6), Kd=KD, on_gpu=True,
+                     max_coils=max_coils)
+
+
+def _images(coils, seed):
+    g = torch.Generator(device="cpu").manual_seed(seed)
+    return torch.randn((coils,) + tuple(reversed(ND)), dtype=torch.complex64, generator=g).cuda()
+
+
+def _samples(coils, M, seed):
+    g = torch.Generator(device="cpu").manual_seed(seed)
+    return torch.randn((coils, M), dtype=torch.complex64, generator=g).cuda()
+
+
+def _per_coil(x, y):
+    """Forward and adjoint of each coil alone on a fresh single-coil operator."""
+    A1 = _operator(1)
+    fw = [A1.plan.forward(x[c:c + 1].contiguous(),
+                          torch.empty((1, A1.M), dtype=torch.complex64, device="cuda"), 1)
+          for c in range(x.shape[0])]
+    ad = [A1.plan.adjoint(y[c:c + 1].contiguous(), torch.empty_like(x[c:c + 1]), 1)
+          for c in range(y.shape[0])]
+    return torch.cat(fw), torch.cat(ad)
+
+
+def _fw(A, x):
+    c = x.shape[0]
+    return A.plan.forward(x.contiguous(), torch.empty((c, A.M), dtype=torch.complex64,
+                                                      device="cuda"), c)
+
+
+def _ad(A, y):
+    c = y.shape[0]
+    return A.plan.adjoint(y.contiguous(), torch.empty((c,) + tuple(reversed(ND)),
+                                                      dtype=torch.complex64, device="cuda"), c)
+
+
+def test_coil_count_changes_between_calls(gpu_lib):
+    A = _operator(COILS)
+    x, y = _images(COILS, 1), _samples(COILS, A.M, 2)
+    y_ref, x_ref = _per_coil(x, y)
+    for c in (COILS, 2, 5, 1, COILS, 3):
+        assert rel_l2(_fw(A, x[:c]).cpu().numpy(), y_ref[:c].cpu().numpy()) < 1e-5, c
+        assert rel_l2(_ad(A, y[:c]).cpu().numpy(), x_ref[:c].cpu().numpy()) < 1e-5, c
+
+
+def test_graph_with_few_coils_replays_after_a_wider_call(gpu_lib):
+    A = _operator(COILS)
+    x, y = _images(COILS, 3), _samples(COILS, A.M, 4)
+    y_ref, x_ref = _per_coil(x, y)
+    c = 2
+    xs, ys = x[:c].contiguous(), y[:c].contiguous()
+    yo = torch.empty((c, A.M), dtype=torch.complex64, device="cuda")
+    xo = torch.empty_like(xs)
+    _fw(A, x)                                  # buffers sized for every coil
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(s):                 # plans and buffers for c coils
+        A.plan.forward(xs, yo, c)
+        A.plan.adjoint(ys, xo, c)
+    torch.cuda.current_stream().wait_stream(s)
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        A.plan.forward(xs, yo, c)
+        A.plan.adjoint(ys, xo, c)
+    for _ in range(2):
+        _fw(A, x)                              # writes rows the graph reads as padding
+        _ad(A, y)
+        yo.zero_()
+        xo.zero_()
+        g.replay()
+        torch.cuda.synchronize()
+        assert rel_l2(yo.cpu().numpy(), y_ref[:c].cpu().numpy()) < 1e-5
+        assert rel_l2(xo.cpu().numpy(), x_ref[:c].cpu().numpy()) < 1e-5
+    np.testing.assert_array_equal(_fw(A, xs).cpu().numpy(), yo.cpu().numpy())
