@@ -115,6 +115,22 @@ int gbn_forward(gbn_plan* plan, const void* x, void* y, int coils,
 int gbn_adjoint(gbn_plan* plan, const void* y, void* x, int coils,
                 void* stream);
 
+/* The same transforms on HOST buffers, as the reference's NufftBase.fft /
+ * NufftBase.adj take and return host arrays (mrrt/nufft/_nufft.py:425-452
+ * and 454-481).  x and y are host pointers in the layouts above (pageable
+ * or pinned); the call copies the input in, transforms on `stream` and
+ * returns once the result is in host memory.  Single-frame batches of 32
+ * coils or more run as a copy / transform pipeline of 16-coil chunks on two
+ * copy streams the plan owns.  Pageable inputs are read in place by a copy
+ * kernel where the device reports cudaDevAttrPageableMemoryAccess, else
+ * copied by the copy engines; pinned outputs let the copies run at the
+ * link's full rate.  Device pointers and calls during graph capture are
+ * rejected.                                                                 */
+int gbn_forward_host(gbn_plan* plan, const void* x_host, void* y_host,
+                     int coils, void* stream);
+int gbn_adjoint_host(gbn_plan* plan, const void* y_host, void* x_host,
+                     int coils, void* stream);
+
 /* Coil-sensitivity (SENSE) forward: y = NUFFT(maps[c] * image[f]) for every
  * frame f and coil c, the coil-map multiply fused into the deapodisation
  * pass (the coil images are never stored).  The MRI system operator of

@@ -68,6 +68,8 @@ SIGNATURES = {
     "gbn_plan_destroy": [_VP],
     "gbn_forward": [_VP, _VP, _VP, _I, _VP],
     "gbn_adjoint": [_VP, _VP, _VP, _I, _VP],
+    "gbn_forward_host": [_VP, _VP, _VP, _I, _VP],
+    "gbn_adjoint_host": [_VP, _VP, _VP, _I, _VP],
     "gbn_interp_forward": [_VP, _VP, _VP, _I, _VP],
     "gbn_interp_adjoint": [_VP, _VP, _VP, _I, _VP],
     "gbn_interp_adjoint_noalloc": [_VP, _VP, _VP, _I, _VP],

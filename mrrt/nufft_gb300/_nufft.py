@@ -426,84 +426,41 @@ class NufftBase(object):
         return x
 
     # -------------------------------------- host arrays: pipelined by coil chunk
-    def _pipeline_chunk(self, reps):
-        """Repetitions per chunk when host arrays are transformed in a copy /
-        compute pipeline, or None to transform the batch in one piece."""
-        return 16 if reps >= 32 else None
-
-    def _copy_streams(self):
-        dev = self._plan.device
-        if getattr(self, "_streams", None) is None:
-            self._streams = (torch.cuda.Stream(device=dev), torch.cuda.Stream(device=dev))
-        return self._streams
-
-    def _pipelined(self, a, forward):
-        """Host numpy in, host numpy out, in chunks of repetitions: chunk k is
-        transformed while chunk k + 1 is copied in and chunk k - 1 copied out
-        (separate copy streams; host-to-device and device-to-host copies run
-        concurrently).  Returns None when the batch is too small to pipeline
-        or the input is not a plain numpy array (the caller then takes the
-        one-piece path, which also raises the reference's errors)."""
+    def _host_transform(self, a, forward):
+        """Host numpy in, host numpy out, through the library's host-buffer
+        entry points: one call copies in, transforms and copies out (large
+        batches as a copy / transform pipeline of coil chunks).  The result
+        lands in pinned memory from torch's caching host allocator, so the
+        copy out runs at the link's rate.  Returns None for inputs this path
+        does not take (device tensors, on_gpu operators, graph capture, sizes
+        that do not divide); the caller's one-piece path then applies and
+        raises the reference's errors."""
         if self.on_gpu or not isinstance(a, np.ndarray) or torch.cuda.is_current_stream_capturing():
             return None
         narg = self.nargin1 if forward else self.M
         lead = self.__Nd if forward else (self.M,)
         out_lead = (self.M,) if forward else self.__Nd
-        if narg == 0 or a.size % narg:
+        if narg == 0 or a.size == 0 or a.size % narg:
             return None
         reps = a.size // narg
-        cs = self._pipeline_chunk(reps)
-        if cs is None:
-            return None
         arr = a if a.dtype == self._cplx_dtype else a.astype(self._cplx_dtype)
         full = tuple(lead) + (reps,)
         arr = np.asfortranarray(arr.reshape(full, order="F") if arr.shape != full else arr)
-        host_in = torch.from_numpy(arr.reshape(-1, order="F")).view(reps, narg)
-        dev, ct = self._plan.device, self._plan.ctype
-        # device staging kept per (direction, reps): no allocation per call
-        key = (forward, reps)
-        bufs = getattr(self, "_pipe_bufs", None)
-        if bufs is None:
-            bufs = self._pipe_bufs = {}
-        if key not in bufs:
-            # one buffer pair per direction: drop the other batch size's
-            for k in [k for k in bufs if k[0] == forward]:
-                del bufs[k]
-            bufs[key] = (torch.empty((reps,) + tuple(reversed(lead)), dtype=ct, device=dev),
-                         torch.empty((reps,) + tuple(reversed(out_lead)), dtype=ct, device=dev))
-        dev_in, dev_out = bufs[key]
-        host_out = torch.empty(dev_out.shape, dtype=ct, pin_memory=True)
-        compute = torch.cuda.current_stream(dev)
-        h2d, d2h = self._copy_streams()
-        # the copies wait for everything queued before this call (including
-        # the previous call's use of the staging buffers)
-        h2d.wait_stream(compute)
-        d2h.wait_stream(compute)
-        for r0 in range(0, reps, cs):
-            r1 = min(reps, r0 + cs)
-            with torch.cuda.stream(h2d):
-                dev_in[r0:r1].view(r1 - r0, -1).copy_(host_in[r0:r1], non_blocking=True)
-                ev_in = torch.cuda.Event()
-                ev_in.record(h2d)
-            compute.wait_event(ev_in)
-            if forward:
-                self._plan.forward(dev_in[r0:r1], dev_out[r0:r1], r1 - r0)
-            else:
-                self._plan.adjoint(dev_in[r0:r1], dev_out[r0:r1], r1 - r0)
-            ev_c = torch.cuda.Event()
-            ev_c.record(compute)
-            with torch.cuda.stream(d2h):
-                d2h.wait_event(ev_c)
-                host_out[r0:r1].copy_(dev_out[r0:r1], non_blocking=True)
-        d2h.synchronize()
+        host_in = torch.from_numpy(arr.reshape(-1, order="F"))
+        host_out = torch.empty((reps,) + tuple(reversed(out_lead)), dtype=self._plan.ctype, pin_memory=True)
+        if forward:
+            self._plan.forward_host(host_in, host_out, reps)
+        else:
+            self._plan.adjoint_host(host_in, host_out, reps)
         nd = len(out_lead) + 1
-        return host_out.numpy().transpose(tuple(reversed(range(nd))))
+        out = host_out.numpy().transpose(tuple(reversed(range(nd))))
+        return out[..., 0] if reps == 1 else out
 
     def fft(self, x):
         """Forward NUFFT (uniform image -> non-uniform samples)."""
         if self.order == "C":
             x = self._swap_reps(x, self.nargin1)
-        out = self._pipelined(x, True)
+        out = self._host_transform(x, True)
         if out is not None:
             return self._unswap_reps(out, self.nargout1) if self.order == "C" else out
         xt, reps = self._device_in(x, self.nargin1, self.__Nd)
@@ -518,7 +475,7 @@ class NufftBase(object):
         """Adjoint NUFFT (non-uniform samples -> uniform image)."""
         if self.order == "C":
             k = self._swap_reps(k, self.nargout1)
-        out = self._pipelined(k, False)
+        out = self._host_transform(k, False)
         if out is not None:
             return self._unswap_reps(out, self.nargin1) if self.order == "C" else out
         yt, reps = self._device_in(k, self.M, (self.M,))

@@ -127,6 +127,38 @@ class GpuPlan:
                                             ctypes.c_void_p(x.data_ptr()), int(coils), _stream()))
         return x
 
+    def _check_host(self, t, numel, name):
+        if not isinstance(t, torch.Tensor) or t.device.type != "cpu":
+            raise ValueError("%s must be a CPU tensor" % name)
+        if t.dtype != self.ctype:
+            raise ValueError("%s must be %s, got %s" % (name, self.ctype, t.dtype))
+        if not t.is_contiguous():
+            raise ValueError("%s must be contiguous" % name)
+        if t.numel() != numel:
+            raise ValueError("%s has %d elements, expected %d" % (name, t.numel(), numel))
+
+    def forward_host(self, x, y, coils):
+        """Forward transform of host memory into host memory (CPU tensors in
+        the device layouts, pageable or pinned); returns when y holds the
+        result."""
+        F = len(self.frame_offsets) - 1
+        self._check_host(x, F * coils * self.Nprod, "x")
+        self._check_host(y, coils * self.M_total, "y")
+        with torch.cuda.device(self.device):
+            _lib.check(self.lib.gbn_forward_host(self.handle, ctypes.c_void_p(x.data_ptr()),
+                                                 ctypes.c_void_p(y.data_ptr()), int(coils), _stream()))
+        return y
+
+    def adjoint_host(self, y, x, coils):
+        """Adjoint transform of host memory into host memory."""
+        F = len(self.frame_offsets) - 1
+        self._check_host(y, coils * self.M_total, "y")
+        self._check_host(x, F * coils * self.Nprod, "x")
+        with torch.cuda.device(self.device):
+            _lib.check(self.lib.gbn_adjoint_host(self.handle, ctypes.c_void_p(y.data_ptr()),
+                                                 ctypes.c_void_p(x.data_ptr()), int(coils), _stream()))
+        return x
+
     def forward_sense(self, image, maps, y, coils):
         """Coil-sensitivity forward: image [F, N...] and maps [coils, N...]
         (plan layout) -> samples, the map multiply fused into the pad."""
