@@ -68,7 +68,16 @@ gather_kernel(const GatherParams<R> p) {
     const int LS = LSC > 0 ? LSC : p.ln.LS;
     const int lsh = LSC > 0 ? (LSC == 32 ? 5 : LSC == 16 ? 4 : LSC == 8 ? 3 : LSC == 4 ? 2 : LSC == 2 ? 1 : 0)
                             : p.ln.lsh;
-    const int LSP = LSC > 0 ? (LSC == 1 ? 1 : LSC + 1) : p.ln.LSP;
+    // Tap split (3-D, 8 coil lanes, even width, single precision): a
+    // half-warp serves one sample, its two 8-lane halves taking the even and
+    // odd taps along axis 0.  Cell rows are 8 coils wide, coil c of a cell at region
+    // x-position x stored at slot c ^ (x & 7): the two cells a half-warp
+    // reads (x and x + 1) then fill complementary halves of the 16 bank pairs,
+    // where two independent samples' padded rows would mostly collide.  In
+    // 2-D (36 taps per sample) the extra per-sample shuffles cost more than
+    // the conflicts, so 2-D keeps four samples per warp.
+    constexpr bool TS = LSC == 8 && NDIM == 3 && JJ > 0 && (JJ % 2) == 0 && sizeof(R) == 4;
+    const int LSP = TS ? 8 : (LSC > 0 ? (LSC == 1 ? 1 : LSC + 1) : p.ln.LSP);
     const int c0 = blockIdx.y << lsh;
     const int nc = min(LS, p.coils - c0);
 
@@ -109,7 +118,7 @@ gather_kernel(const GatherParams<R> p) {
                         w.x = w.x / p.grid_scale;
                         w.y = w.y / p.grid_scale;
                     }
-                    S[dst + c + u] = w;
+                    S[dst + (TS ? ((c + u) ^ (r[0] & 7)) : c + u)] = w;
                 }
             }
         }
@@ -119,8 +128,9 @@ gather_kernel(const GatherParams<R> p) {
     // ---- per-sample gather from shared memory -------------------------------
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int nwarps = blockDim.x >> 5;
-    const int SW = 32 >> lsh;
-    const int slot = lane >> lsh, coil = lane & (LS - 1);
+    const int SW = TS ? 2 : 32 >> lsh;
+    const int slot = TS ? lane >> 4 : lane >> lsh, coil = lane & (LS - 1);
+    const int th = TS ? (lane >> 3) & 1 : 0;   // tap half (tap split)
     const int64_t fo = p.foff[f];
     const int Mf = (int)(p.foff[f + 1] - fo);
     C* yb = p.y + fo * p.coils + (int64_t)(c0 + coil) * Mf;
@@ -136,6 +146,7 @@ gather_kernel(const GatherParams<R> p) {
         const int nb = min(32, count - base);
         R mcr[NDIM][JL], mci[NDIM][JL];
         int mbase = 0;  // shared-memory index of the window's first cell
+        int mx0 = 0;    // region x-position of the window's first cell
         int midx = 0;
         C mph = cmake<R>((R)1, (R)0);
 #pragma unroll
@@ -166,6 +177,7 @@ gather_kernel(const GatherParams<R> p) {
                         if (JJ > 0 || j < g.J[d]) table_coef<R, CX>(g, d, tt[d], kf[d] + j, mcr[d][j], mci[d][j]);
             }
             mbase = ((loc[2] * Rd[1] + loc[1]) * Rd[0] + loc[0]) * LSP;
+            mx0 = loc[0];
             if (p.apply_ph) mph = p.s.ph[e];
         }
         for (int s0 = 0; s0 < nb; s0 += SW) {
@@ -190,14 +202,47 @@ gather_kernel(const GatherParams<R> p) {
             for (int d = 0; d < NDIM; ++d)
 #pragma unroll
                 for (int j = 0; j < JL; ++j) q[d][j] = CX ? cmake<R>(cr[d][j], ci[d][j]) : cmake<R>(cr[d][j], cr[d][j]);
-            const int sbase = __shfl_sync(0xffffffffu, mbase, src) + coil;
+            const int sbase = __shfl_sync(0xffffffffu, mbase, src) + (TS ? 0 : coil);
+            const int x0 = TS ? __shfl_sync(0xffffffffu, mx0, src) : 0;
             const int idx = __shfl_sync(0xffffffffu, midx, src);
             C ph;
             ph.x = __shfl_sync(0xffffffffu, mph.x, src);
             ph.y = __shfl_sync(0xffffffffu, mph.y, src);
-            if (src >= nb) continue;
 
             C acc = cmake<R>((R)0, (R)0);
+            if constexpr (TS) {
+                // lanes past the last sample run on zero coefficients (their
+                // window is cell 0) so that the whole warp reaches the shuffle
+                constexpr int JH = (JJ > 0 ? JJ : 2) / 2;
+                int off[JH];
+                C qh[JH];
+#pragma unroll
+                for (int jj = 0; jj < JH; ++jj) {
+                    const int j0 = 2 * jj + th;
+                    off[jj] = j0 * 8 + (coil ^ ((x0 + j0) & 7));
+                    qh[jj] = th ? q[0][2 * jj + 1] : q[0][2 * jj];
+                }
+#pragma unroll
+                for (int j2 = 0; j2 < (NDIM > 2 ? JL : 1); ++j2) {
+                    C plane = cmake<R>((R)0, (R)0);
+#pragma unroll
+                    for (int j1 = 0; j1 < JL; ++j1) {
+                        const int rb = sbase + j2 * planestride + j1 * rowstride;
+                        C row = cmake<R>((R)0, (R)0);
+#pragma unroll
+                        for (int jj = 0; jj < JH; ++jj) qfma<CX>(row, qh[jj], S[rb + off[jj]]);
+                        qfma<CX>(plane, q[NDIM > 1 ? 1 : 0][j1], row);
+                    }
+                    if (NDIM > 2)
+                        qfma<CX>(acc, q[NDIM > 2 ? 2 : 0][j2], plane);
+                    else
+                        acc = plane;
+                }
+                acc.x += __shfl_xor_sync(0xffffffffu, acc.x, 8);
+                acc.y += __shfl_xor_sync(0xffffffffu, acc.y, 8);
+                if (src >= nb || th) continue;
+            } else {
+            if (src >= nb) continue;
             if (NDIM == 1) {
 #pragma unroll
                 for (int j0 = 0; j0 < JL; ++j0)
@@ -233,6 +278,7 @@ gather_kernel(const GatherParams<R> p) {
                         qfma<CX>(acc, q[NDIM > 2 ? 2 : 0][j2], plane);
                     }
                 }
+            }
             }
             if (coil < nc) {
                 if (p.apply_ph) acc = cmul(acc, ph);
@@ -271,6 +317,16 @@ size_t gather_smem(const Geom<R>& g, const Lanes& ln) {
     return cells * (size_t)ln.LSP * sizeof(typename Cx<R>::T);
 }
 
+// Shared memory of one launch: the tap-split kernels keep unpadded 8-coil rows.
+template <typename R, int NDIM, int JJ, int LSC>
+static size_t gather_smem_of(const Geom<R>& g, const Lanes& ln) {
+    constexpr bool TS = LSC == 8 && NDIM == 3 && JJ > 0 && (JJ % 2) == 0 && sizeof(R) == 4;
+    if (!TS) return gather_smem(g, ln);
+    size_t cells = 1;
+    for (int d = 0; d < g.ndim; ++d) cells *= (size_t)(g.T[d] + g.J[d] - 1);
+    return cells * 8 * sizeof(typename Cx<R>::T);
+}
+
 template <typename K>
 static cudaError_t ensure_smem(K kernel, size_t bytes) {
     return ensure_dynamic_smem(reinterpret_cast<const void*>(kernel), bytes);
@@ -278,7 +334,7 @@ static cudaError_t ensure_smem(K kernel, size_t bytes) {
 
 template <typename R, int NDIM, bool CX, int JJ, int LSC>
 static cudaError_t gather_launch(const GatherParams<R>& p, cudaStream_t s) {
-    const size_t smem = gather_smem(p.g, p.ln);
+    const size_t smem = gather_smem_of<R, NDIM, JJ, LSC>(p.g, p.ln);
     cudaError_t e = ensure_smem(gather_kernel<R, NDIM, CX, JJ, LSC>, smem);
     if (e != cudaSuccess) return e;
     dim3 grid(p.nitems, (p.coils + p.ln.LS - 1) / p.ln.LS);

@@ -368,3 +368,25 @@ def test_exported_dtft_matches_reference(gpu_lib):
     xa = dtft_adj(c["y"], c["omega"], shape=c["Nd"], n_shift=c["n_shift"])
     assert rel_l2(xa, g["dtft_xadj"]) < 1e-12
 
+
+
+@pytest.mark.parametrize("Nd,Kd,J", [((40, 36), (80, 72), 6), ((20, 18, 16), (40, 36, 32), 6),
+                                     ((20, 18, 16), (40, 36, 32), 4)])
+@pytest.mark.parametrize("coils", [8, 7])
+def test_eight_coil_batches_match_oracle(gpu_lib, Nd, Kd, J, coils):
+    """Batches of 5-8 coils run the gather with 8 coil lanes (four samples
+    per warp in 2-D; in 3-D two, each sample's taps along axis 0 split
+    between two half-warps); against the oracle, for a full and a partial
+    coil chunk."""
+    from mrrt.nufft_gb300 import NufftBase
+
+    rng = np.random.default_rng(5)
+    M = 3000
+    omega = rng.uniform(-np.pi, np.pi, (M, len(Nd)))
+    kw = dict(Nd=Nd, omega=omega, Jd=(J,) * len(Nd), Kd=Kd)
+    A = NufftBase(max_coils=coils, **kw)
+    B = O.OracleNufft(**kw)
+    x = (rng.standard_normal(Nd + (coils,)) + 1j * rng.standard_normal(Nd + (coils,))).astype(np.complex64)
+    y = B.fft(x)
+    assert rel_l2(A.fft(x), y) < 1e-5
+    assert rel_l2(A.adj(y), B.adj(y)) < 1e-5
