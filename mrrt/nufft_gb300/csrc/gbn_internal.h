@@ -49,7 +49,7 @@ struct Geom {
 // SW = 32 / LS samples per warp.  Staged grid values for one cell occupy
 // LSP complex slots (LS + 1 for LS > 1: conflict-free transposed staging).
 struct Lanes {
-    int LS, lsh, LSP, swz;
+    int LS, lsh, LSP;
 };
 
 // Sorted sample list (one per direction).

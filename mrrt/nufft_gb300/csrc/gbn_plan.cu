@@ -91,7 +91,6 @@ Lanes make_lanes(int ndim, int coils) {
     ln.LS = std::min(lane_cap(ndim), next_pow2(std::max(coils, 1)));
     ln.lsh = ilog2(ln.LS);
     ln.LSP = ln.LS == 1 ? 1 : ln.LS + 1;
-    ln.swz = 0;
     return ln;
 }
 
@@ -203,8 +202,6 @@ Geom<R> make_geom(const gbn_plan* P, bool spread) {
     std::memset(&g, 0, sizeof(g));
     const gbn_geometry& G = P->geom;
     g.ndim = G.ndim;
-    const int64_t tab_stride = 0;
-    (void)tab_stride;
     const R* base = reinterpret_cast<const R*>(P->tables.p);
     size_t off = 0;
     for (int d = 0; d < 3; ++d) {
