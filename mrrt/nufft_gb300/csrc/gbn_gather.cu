@@ -54,6 +54,13 @@ __device__ __forceinline__ void load_coefs(const R* src, const Geom<R>& g, R (&c
     }
 }
 
+// Element-wise staging (per-cell offsets and phases in shared memory, then
+// one thread per staged value): the 2-D kernels with 16 or 32 coil lanes
+// (2-D workload gather 0.134 -> 0.128 ms).  With 8 lanes the extra shared
+// memory cost more than the balanced loads gained (series gather 0.413 ->
+// 0.448 ms), and in 3-D it would leave one CTA per SM.
+__host__ __device__ constexpr bool gather_elem_staging(int ndim, int lsc) { return ndim == 2 && lsc >= 16; }
+
 template <typename R, int NDIM, bool CX, int JJ, int LSC>
 __global__ void __launch_bounds__(GATHER_THREADS)
 gather_kernel(const GatherParams<R> p) {
@@ -77,6 +84,7 @@ gather_kernel(const GatherParams<R> p) {
     // 2-D (36 taps per sample) the extra per-sample shuffles cost more than
     // the conflicts, so 2-D keeps four samples per warp.
     constexpr bool TS = LSC == 8 && NDIM == 3 && JJ > 0 && (JJ % 2) == 0 && sizeof(R) == 4;
+    constexpr bool ES = gather_elem_staging(NDIM, LSC);
     const int LSP = TS ? 8 : (LSC > 0 ? (LSC == 1 ? 1 : LSC + 1) : p.ln.LSP);
     const int c0 = blockIdx.y << lsh;
     const int nc = min(LS, p.coils - c0);
@@ -86,9 +94,60 @@ gather_kernel(const GatherParams<R> p) {
     int Rd[3];
     const int Rtot = region_dims(g, NDIM, Rd);
 
-    // ---- stage tile + halo for nc coils: thread per cell, coils in batches
-    // of four independent loads ----------------------------------------------
+    // ---- stage tile + halo for nc coils --------------------------------------
     const C* gb = p.grid + ((int64_t)f * p.coils + c0) * g.gsp;
+    if constexpr (ES) {
+        // (1) thread per cell: grid offset and phase_before into shared
+        // memory; (2) thread per (coil, cell), consecutive threads on
+        // consecutive cells, eight independent loads in flight.  Every
+        // thread gets the same share of loads, where a thread per cell
+        // serialises all the coils of its cells.
+        int64_t* soff = reinterpret_cast<int64_t*>(S + (size_t)Rtot * LSP);
+        C* sph = reinterpret_cast<C*>(soff + Rtot);
+        for (int cell = threadIdx.x; cell < Rtot; cell += blockDim.x) {
+            int r[3];
+            int rem = cell;
+            r[0] = rem % Rd[0];
+            rem /= Rd[0];
+            r[1] = rem % Rd[1];
+            r[2] = rem / Rd[1];
+            int k[3] = {0, 0, 0};
+#pragma unroll
+            for (int d = 0; d < NDIM; ++d) k[d] = wrapk(org[d] + r[d], g.K[d]);
+            soff[cell] = k[0] + (int64_t)k[1] * g.gs1 + (int64_t)k[2] * g.gs2;
+            if (p.apply_pb) sph[cell] = phase_before(g, k);
+        }
+        __syncthreads();
+        const int E = Rtot * nc;
+        const int step = blockDim.x;
+        int cell = threadIdx.x, c = 0;
+        while (cell >= Rtot && c < nc) cell -= Rtot, ++c;
+        for (int e = threadIdx.x; e < E; e += 8 * step) {
+            C v[8];
+            int cc[8], cl[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                cc[u] = c;
+                cl[u] = cell;
+                if (e + u * step < E) v[u] = gb[(int64_t)c * g.gsp + soff[cell]];
+                cell += step;
+                while (cell >= Rtot) cell -= Rtot, ++c;
+            }
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                if (e + u * step < E) {
+                    C w = v[u];
+                    if (p.apply_pb) w = cmul(w, sph[cl[u]]);
+                    if (p.grid_scale != (R)1) {
+                        w.x = w.x / p.grid_scale;
+                        w.y = w.y / p.grid_scale;
+                    }
+                    S[cl[u] * LSP + cc[u]] = w;
+                }
+            }
+        }
+    } else {
+    // thread per cell, coils in batches of four independent loads
     for (int cell = threadIdx.x; cell < Rtot; cell += blockDim.x) {
         int r[3];
         int rem = cell;
@@ -122,6 +181,7 @@ gather_kernel(const GatherParams<R> p) {
                 }
             }
         }
+    }
     }
     __syncthreads();
 
@@ -321,10 +381,12 @@ size_t gather_smem(const Geom<R>& g, const Lanes& ln) {
 template <typename R, int NDIM, int JJ, int LSC>
 static size_t gather_smem_of(const Geom<R>& g, const Lanes& ln) {
     constexpr bool TS = LSC == 8 && NDIM == 3 && JJ > 0 && (JJ % 2) == 0 && sizeof(R) == 4;
-    if (!TS) return gather_smem(g, ln);
     size_t cells = 1;
     for (int d = 0; d < g.ndim; ++d) cells *= (size_t)(g.T[d] + g.J[d] - 1);
-    return cells * 8 * sizeof(typename Cx<R>::T);
+    if (TS) return cells * 8 * sizeof(typename Cx<R>::T);
+    if (gather_elem_staging(NDIM, LSC))   // + per-cell grid offset and phase
+        return gather_smem(g, ln) + cells * sizeof(int64_t) + cells * sizeof(typename Cx<R>::T);
+    return gather_smem(g, ln);
 }
 
 template <typename K>
