@@ -451,6 +451,17 @@ def run_ours(args, rank, world):
     t_e2e = (time.perf_counter() - t0) / e2e_steps
     h2d = x_f.nbytes + yh.nbytes
     d2h = yh.nbytes + xh.nbytes
+    # the host path's results against the device path on the same images
+    # (the pipelined chunks run their FFTs 16 planes at a time)
+    P.forward(x_dev, y_dev, C)
+    P.adjoint(y_dev, xa_dev, C)
+    e_f = oracle.rel_l2(np.asarray(yh).T.reshape(-1), y_dev.reshape(-1).cpu().numpy())
+    e_a = oracle.rel_l2(np.asarray(Ah.adj(np.asarray(y_dev.cpu().numpy().T))).ravel(order="F"),
+                        xa_dev.cpu().numpy().transpose(tuple(range(nd, -1, -1))).ravel(order="F"))
+    if not (e_f < 1e-6 and e_a < 1e-6):
+        print("bench.py: end-to-end results differ from the device path: %.3g %.3g" % (e_f, e_a),
+              file=sys.stderr, flush=True)
+        raise SystemExit(1)
 
     if rank != 0:
         return
@@ -619,31 +630,60 @@ def run_series(args, rank, world):
     y_pin = torch.empty((C * S.M_total,), dtype=torch.complex64).pin_memory()
     xa_pin = torch.empty_like(x_pin).pin_memory()
 
-    # the samples leave on a copy stream while the adjoint runs (it only
-    # reads them); the images leave after it
+    # A stream of independent series: every step copies its images in from
+    # pinned host memory and reads its samples and adjoint images back.  The
+    # copies run on two copy streams beside the graphs: step k + 1's images
+    # come in and step k's samples go out while step k's adjoint runs; step
+    # k's images go out while step k + 1's forward runs.  The timed region
+    # ends when the last step's results are in host memory.
+    h2d = torch.cuda.Stream(device=dev)
     d2h = torch.cuda.Stream(device=dev)
-    fwd_done = torch.cuda.Event()
+    ev_in, ev_fwd, ev_adj, ev_y, ev_xa = (torch.cuda.Event() for _ in range(5))
 
-    def e2e():
+    def e2e_run(steps):
         main = torch.cuda.current_stream()
-        S.x_static.copy_(x_pin, non_blocking=True)
-        S.replay_forward()
-        fwd_done.record(main)
-        d2h.wait_event(fwd_done)
-        with torch.cuda.stream(d2h):
-            y_pin.copy_(S.y_static, non_blocking=True)
-        S.replay_adjoint()
-        xa_pin.copy_(S.xa_static, non_blocking=True)
-        main.wait_stream(d2h)   # the next step's forward rewrites the samples
+        h2d.wait_stream(main)
+        d2h.wait_stream(main)
+        with torch.cuda.stream(h2d):
+            S.x_static.copy_(x_pin, non_blocking=True)
+            ev_in.record(h2d)
+        for k in range(steps):
+            main.wait_event(ev_in)              # this step's images are in
+            if k > 0:
+                main.wait_event(ev_y)           # previous samples read out
+            S.replay_forward()
+            ev_fwd.record(main)
+            if k + 1 < steps:                   # next step's images
+                h2d.wait_event(ev_fwd)
+                with torch.cuda.stream(h2d):
+                    S.x_static.copy_(x_pin, non_blocking=True)
+                    ev_in.record(h2d)
+            d2h.wait_event(ev_fwd)
+            with torch.cuda.stream(d2h):
+                y_pin.copy_(S.y_static, non_blocking=True)
+                ev_y.record(d2h)
+            if k > 0:
+                main.wait_event(ev_xa)          # previous images read out
+            S.replay_adjoint()
+            ev_adj.record(main)
+            d2h.wait_event(ev_adj)
+            with torch.cuda.stream(d2h):
+                xa_pin.copy_(S.xa_static, non_blocking=True)
+                ev_xa.record(d2h)
+        d2h.synchronize()
         main.synchronize()
 
-    for _ in range(3):
-        e2e()
+    e2e_run(3)
     e2e_steps = max(10, args.steps)
     t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        e2e()
+    e2e_run(e2e_steps)
     t_e2e = (time.perf_counter() - t0) / e2e_steps
+    # the overlapped copies must deliver exactly the eager transforms' results
+    y_ref = S.forward(x_dev)
+    xa_ref = S.adjoint(y_ref)
+    if not (torch.equal(y_pin, y_ref.reshape(-1).cpu()) and torch.equal(xa_pin, xa_ref.cpu())):
+        print("bench.py: end-to-end results differ from the eager transform", file=sys.stderr, flush=True)
+        raise SystemExit(1)
 
     if rank != 0:
         return
