@@ -304,7 +304,8 @@ def config_dict(extra=None):
 
 
 def _clock_path(rank):
-    out = os.path.join(HERE, "gpurun_out")
+    """Where the clock sampler writes: $GBN_BENCH_OUT, else the working directory."""
+    out = os.environ.get("GBN_BENCH_OUT", ".")
     return os.path.join(out if os.path.isdir(out) else ".", "clocks_rank%d.csv" % rank)
 
 

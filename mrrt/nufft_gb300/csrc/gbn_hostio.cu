@@ -2,7 +2,7 @@
 // place.  On a system whose GPU shares the host's page tables (the device
 // attribute cudaDevAttrPageableMemoryAccess is 1, e.g. Grace over
 // NVLink-C2C) this moves a caller's ordinary (unpinned) array at the link's
-// rate without the driver's staging through pinned bounce buffers, and,
+// rate without the CUDA driver's staging through pinned bounce buffers, and,
 // unlike a copy from pageable memory, it does not hold the calling thread
 // while the data move.  The host-buffer transforms use it for inputs that
 // are not pinned; pinned inputs and every output go through the copy engines.

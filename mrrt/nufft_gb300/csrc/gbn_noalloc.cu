@@ -6,7 +6,7 @@
 // with cudaMalloc.  Callers that cannot allocate during a call (a fixed
 // device-memory budget, or no room for the device-wide synchronisation a
 // cudaMalloc / cudaFree may cause) use this array instead: it is part of the
-// module image, so the driver reserves it when the module loads and no
+// module image, so the CUDA driver reserves it when the module loads and no
 // allocator is ever called for it.
 //
 // The array lives in its own translation unit so that the module holding it
