@@ -212,9 +212,9 @@ int gbn_grad_tm(gbn_plan* plan, const void* grid, const void* gy,
                 const double* phase_shift, void* gtm, int coils, void* stream);
 
 /* Device pointer of the plan's forward grid buffer (valid until the next
- * call on the plan).  Its layout is the transform's own: [coils][K...] for
- * 1-D and 3-D plans, [K1][coils][K0] for 2-D plans (row k1 of every coil
- * plane together, so the FFT's row pass skips the zero-padded rows).  The
+ * call on the plan).  Its layout is the transform's own: [K1][coils][K0] for
+ * 2-D plans (row k1 of every coil plane together, so the FFT's row pass skips
+ * the zero-padded rows), [coils][K...] for 1-D and 3-D plans.  The
  * interpolation-only entry points keep the [planes][K...] layout.           */
 int gbn_forward_grid(gbn_plan* plan, void** grid);
 

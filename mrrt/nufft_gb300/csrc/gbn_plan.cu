@@ -166,8 +166,10 @@ struct gbn_plan {
     int n_gitems = 0, n_sitems = 0, n_rtiles = 0, n_slots = 0;
     int64_t glen = 0, slen = 0;
     DevBuf pad, grid, scratch;
-    DevBuf mid;           // 2-D: output of the forward's row pass (rows >= N1 stay zero)
-    int64_t mid_clean = 0;     // rows of K0 cells from which mid is known to be zero
+    DevBuf mid;           // output of the forward's slab pass (2-D rows, 3-D z-planes); the
+                          // slabs >= N_last the last-axis pass reads stay zero
+    int64_t mid_clean = 0;     // 2-D: slabs from which mid is known to be zero
+    int mid_planes = 0;        // planes the mid buffer holds
     int cap_planes = 0;        // planes the pad/grid buffers hold
     int64_t scratch_cap = 0;   // complex elements
     std::vector<FftEntry> ffts;
@@ -229,7 +231,7 @@ Geom<R> make_geom(const gbn_plan* P, bool spread) {
     g.Kprod = P->Kprod;
     g.Nprod = P->Nprod;
     // plane-major layout (the C ABI's grids); transform-internal grids of
-    // 2-D plans are re-strided by internal_layout
+    // 2-D and 3-D plans are re-strided by internal_layout
     g.gsp = P->Kprod;
     g.gs1 = g.K[0];
     g.gs2 = (int64_t)g.K[0] * g.K[1];
@@ -240,18 +242,31 @@ Geom<R> make_geom(const gbn_plan* P, bool spread) {
 // r of every plane is one contiguous block, so the row FFT pass runs over the
 // first N1 * planes rows only (the others hold zero padding on the way in and
 // are cropped away on the way out) and the column pass is one strided batch.
-bool pruned_2d(const gbn_plan* P) { return P->geom.ndim == 2; }
+// The 3-D transform keeps the plane-major layout and prunes plane by plane
+// (up to PRUNE3_MAX_PLANES planes): a batched 2-D FFT of the first N2
+// z-planes, then the z-pass at the plane's own stride.  Interleaving z-planes
+// too would stretch the z-pass's stride to planes x K1 x K0, which measured
+// slower than the pruning saves.
+constexpr int PRUNE3_MAX_PLANES = 16;
+bool pruned_3d(const gbn_plan* P, int planes) { return P->geom.ndim == 3 && planes <= PRUNE3_MAX_PLANES; }
+
+// cells of one slab (a row in 2-D, a z-plane in 3-D), and the image extent
+// along the last axis
+int64_t slab_cells(const gbn_plan* P) {
+    return P->geom.ndim == 2 ? P->geom.Kd[0] : (int64_t)P->geom.Kd[0] * P->geom.Kd[1];
+}
+int last_n(const gbn_plan* P) { return P->geom.Nd[P->geom.ndim - 1]; }
 
 template <typename T>
 void internal_layout(const gbn_plan* P, int planes, T& g) {
-    if (pruned_2d(P)) {
+    if (P->geom.ndim == 2) {
         g.gsp = P->geom.Kd[0];
         g.gs1 = (int64_t)planes * P->geom.Kd[0];
         g.gs2 = 0;
     } else {
         g.gsp = P->Kprod;
         g.gs1 = P->geom.Kd[0];
-        g.gs2 = P->geom.ndim > 2 ? (int64_t)P->geom.Kd[0] * P->geom.Kd[1] : 0;
+        g.gs2 = P->geom.ndim > 2 ? slab_cells(P) : 0;
     }
 }
 
@@ -634,14 +649,19 @@ int ensure_buffers(gbn_plan* P, int coils) {
         if (e != cudaSuccess) return cuda_fail(e, "pad buffer clear");
         e = P->grid.alloc(bytes);
         if (e != cudaSuccess) return fail(GBN_ERR_NOMEM, "grid buffer allocation failed");
-        if (pruned_2d(P)) {
-            e = P->mid.alloc(bytes);
-            if (e != cudaSuccess) return fail(GBN_ERR_NOMEM, "row-pass buffer allocation failed");
-            e = cudaMemset(P->mid.p, 0, bytes);
-            if (e != cudaSuccess) return cuda_fail(e, "row-pass buffer clear");
-            P->mid_clean = 0;
-        }
         P->cap_planes = planes;
+    }
+    // the pruned FFT's intermediate buffer: every plane in 2-D, the planes of
+    // a pruned call in 3-D (none beyond PRUNE3_MAX_PLANES)
+    const int mid_need = P->geom.ndim == 2 || pruned_3d(P, planes) ? planes : 0;
+    if (mid_need > P->mid_planes) {
+        const size_t bytes = (size_t)mid_need * P->Kprod * csz;
+        cudaError_t e = P->mid.alloc(bytes);
+        if (e != cudaSuccess) return fail(GBN_ERR_NOMEM, "slab-pass buffer allocation failed");
+        e = cudaMemset(P->mid.p, 0, bytes);
+        if (e != cudaSuccess) return cuda_fail(e, "slab-pass buffer clear");
+        P->mid_planes = mid_need;
+        P->mid_clean = 0;
     }
     return ensure_scratch(P, coils);
 }
@@ -656,18 +676,22 @@ int get_fft(gbn_plan* P, int planes, FftEntry** out) {
     const cufftType type = P->dbl ? CUFFT_Z2Z : CUFFT_C2C;
     FftEntry f{planes, 0, 0, 0};
     cufftResult r;
-    if (pruned_2d(P)) {
-        const int K0 = G.Kd[0], K1 = G.Kd[1], N1 = G.Nd[1];
-        int nx[1] = {K0}, ny[1] = {K1};
-        // rows k1 < N1 of every plane: N1 * planes contiguous rows of K0
-        r = cufftPlanMany(&f.hx, 1, nx, nullptr, 1, K0, nullptr, 1, K0, type, N1 * planes);
-        if (r != CUFFT_SUCCESS) return cufft_fail(r, "cufftPlanMany (rows)");
-        // every column (plane, k0): stride planes * K0 between k1, adjacent columns
-        int emb[1] = {K1};
-        r = cufftPlanMany(&f.hy, 1, ny, emb, planes * K0, 1, emb, planes * K0, 1, type, planes * K0);
+    if (G.ndim == 2 || pruned_3d(P, planes)) {
+        // 2-D: all planes' rows at once (interleaved layout); 3-D: one plane
+        // at a time (its z-planes are contiguous, plane-major layout)
+        const int slab = (int)slab_cells(P), Kl = G.Kd[G.ndim - 1], Nl = last_n(P);
+        const int batch_planes = G.ndim == 2 ? planes : 1;
+        // slabs k < N_last: transformed as rows (2-D) or as K1 x K0 planes (3-D)
+        int nx[2] = {G.ndim == 2 ? G.Kd[0] : G.Kd[1], G.Kd[0]};
+        r = cufftPlanMany(&f.hx, G.ndim - 1, nx, nullptr, 1, slab, nullptr, 1, slab, type, Nl * batch_planes);
+        if (r != CUFFT_SUCCESS) return cufft_fail(r, "cufftPlanMany (slabs)");
+        // every column along the last axis: stride batch_planes * slab, adjacent columns
+        const int zs = batch_planes * slab;
+        int ny[1] = {Kl}, emb[1] = {Kl};
+        r = cufftPlanMany(&f.hy, 1, ny, emb, zs, 1, emb, zs, 1, type, zs);
         if (r != CUFFT_SUCCESS) {
             cufftDestroy(f.hx);
-            return cufft_fail(r, "cufftPlanMany (columns)");
+            return cufft_fail(r, "cufftPlanMany (last axis)");
         }
     } else {
         int n[3];
@@ -691,25 +715,39 @@ int exec_fft(gbn_plan* P, cufftHandle h, void* in, void* out, int dir, cudaStrea
     return GBN_OK;
 }
 
-// Forward Kd-point FFT of the padded planes into the grid.  2-D: the row
-// pass only over the N1 rows that hold data (pad -> mid), then the column
-// pass over every column (mid -> grid).
+// Forward Kd-point FFT of the padded planes into the grid.  2-D and 3-D:
+// the slab pass only over the N_last slabs that hold data (pad -> mid), then
+// the last-axis pass over every column (mid -> grid).
 int fft_forward(gbn_plan* P, int planes, cudaStream_t s) {
     FftEntry* f = nullptr;
     int rc = get_fft(P, planes, &f);
     if (rc) return rc;
-    if (pruned_2d(P)) {
-        // The column pass reads rows [N1 * planes, K1 * planes) of mid as
-        // zero.  A call with more planes wrote rows below N1 * cap_planes, so
-        // rows in [N1 * planes, mid_clean) are cleared first.  A stream being
-        // captured into a graph clears up to N1 * cap_planes on every replay,
-        // since eager calls between replays may write there.
-        const int64_t row = (int64_t)P->geom.Kd[0] * 2 * P->rsize;
-        const int64_t lo = (int64_t)P->geom.Nd[1] * planes;
+    if (pruned_3d(P, planes)) {
+        // the first N2 z-planes of each plane into mid, whose other z-planes
+        // are never written and stay zero; then each plane's z-pass
+        const size_t pb = (size_t)P->Kprod * 2 * P->rsize;
+        char* pad = static_cast<char*>(P->pad.p);
+        char* mid = static_cast<char*>(P->mid.p);
+        char* grid = static_cast<char*>(P->grid.p);
+        for (int pl = 0; pl < planes; ++pl)
+            if ((rc = exec_fft(P, f->hx, pad + pl * pb, mid + pl * pb, CUFFT_FORWARD, s))) return rc;
+        for (int pl = 0; pl < planes; ++pl)
+            if ((rc = exec_fft(P, f->hy, mid + pl * pb, grid + pl * pb, CUFFT_FORWARD, s))) return rc;
+        return GBN_OK;
+    }
+    if (P->geom.ndim == 2) {
+        // The last-axis pass reads slabs [N_last * planes, K_last * planes)
+        // of mid as zero.  A call with more planes wrote slabs below
+        // N_last * cap_planes, so slabs in [N_last * planes, mid_clean) are
+        // cleared first.  A stream being captured into a graph clears up to
+        // N_last * cap_planes on every replay, since eager calls between
+        // replays may write there.
+        const int64_t row = slab_cells(P) * 2 * P->rsize;
+        const int64_t lo = (int64_t)last_n(P) * planes;
         cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
         GBN_CUDA(cudaStreamIsCapturing(s, &cs), "capture status");
         const bool capturing = cs != cudaStreamCaptureStatusNone;
-        const int64_t hi = capturing ? (int64_t)P->geom.Nd[1] * P->cap_planes : P->mid_clean;
+        const int64_t hi = capturing ? (int64_t)last_n(P) * P->mid_planes : P->mid_clean;
         if (hi > lo)
             GBN_CUDA(cudaMemsetAsync(static_cast<char*>(P->mid.p) + lo * row, 0, (size_t)((hi - lo) * row), s),
                      "row-pass buffer clear");
@@ -720,13 +758,22 @@ int fft_forward(gbn_plan* P, int planes, cudaStream_t s) {
     return exec_fft(P, f->h, P->pad.p, P->grid.p, CUFFT_FORWARD, s);
 }
 
-// Inverse FFT of the grid in place.  2-D: every column, then only the N1 rows
-// the crop reads.
+// Inverse FFT of the grid in place.  2-D and 3-D: every column along the
+// last axis, then only the N_last slabs the crop reads.
 int fft_inverse(gbn_plan* P, int planes, cudaStream_t s) {
     FftEntry* f = nullptr;
     int rc = get_fft(P, planes, &f);
     if (rc) return rc;
-    if (pruned_2d(P)) {
+    if (pruned_3d(P, planes)) {
+        const size_t pb = (size_t)P->Kprod * 2 * P->rsize;
+        char* grid = static_cast<char*>(P->grid.p);
+        for (int pl = 0; pl < planes; ++pl)
+            if ((rc = exec_fft(P, f->hy, grid + pl * pb, grid + pl * pb, CUFFT_INVERSE, s))) return rc;
+        for (int pl = 0; pl < planes; ++pl)
+            if ((rc = exec_fft(P, f->hx, grid + pl * pb, grid + pl * pb, CUFFT_INVERSE, s))) return rc;
+        return GBN_OK;
+    }
+    if (P->geom.ndim == 2) {
         if ((rc = exec_fft(P, f->hy, P->grid.p, P->grid.p, CUFFT_INVERSE, s))) return rc;
         return exec_fft(P, f->hx, P->grid.p, P->grid.p, CUFFT_INVERSE, s);
     }

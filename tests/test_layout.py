@@ -1,11 +1,13 @@
-"""2-D plans keep their transform grid row-interleaved, [K1][planes][K0], so
-the FFT's row pass runs over the N1 rows that hold data only.  The column
-pass then reads the other rows of its input as zero.  These tests change the
-coil count between calls (a call with more coil planes writes rows that a call
-with fewer reads as padding) and replay a CUDA graph captured with few coils
-after an eager call with more; every result must equal single-coil calls on a
-fresh operator.  A non-square image and grid catch swapped axes.  Grids of
-several row lengths, in both precisions, are checked against the oracle."""
+"""The pruned FFTs.  2-D plans keep their transform grids row-interleaved,
+[K1][planes][K0], so the row pass runs over the N1 rows that hold data only
+and the column pass reads the other rows of its input as zero.  3-D plans
+prune plane by plane: a 2-D FFT of the first N2 z-planes, then the z-pass.
+These tests change the coil count between calls (in 2-D a call with more
+coil planes writes rows that a call with fewer reads as padding) and replay a
+CUDA graph captured with few coils after an eager call with more; every
+result must equal single-coil calls on a fresh operator.  Non-square images
+and grids catch swapped axes.  Grids of several sizes, in both precisions,
+are checked against the oracle."""
 import numpy as np
 import pytest
 import torch
@@ -14,20 +16,29 @@ from tests.conftest import rel_l2
 
 pytestmark = pytest.mark.gpu
 
-ND, KD, COILS = (40, 48), (80, 96), 6
+COILS = 6
+GEOMS = {
+    "2d": ((40, 48), (80, 96)),
+    "3d": ((20, 16, 12), (40, 32, 24)),
+}
 
 
-def _operator(max_coils):
+def _operator(geom, max_coils):
     from mrrt.nufft_gb300 import NufftBase
-    from mrrt.nufft_gb300.trajectories import radial_2d
 
-    return NufftBase(ND, radial_2d(21, 96, golden=True), Jd=(6, 6), Kd=KD, on_gpu=True,
-                     max_coils=max_coils)
+    Nd, Kd = GEOMS[geom]
+    rng = np.random.default_rng(len(Nd))
+    omega = rng.uniform(-np.pi, np.pi, (2000, len(Nd)))
+    return NufftBase(Nd, omega, Jd=(6,) * len(Nd), Kd=Kd, on_gpu=True, max_coils=max_coils)
 
 
-def _images(coils, seed):
+def _image_shape(geom, coils):
+    return (coils,) + tuple(reversed(GEOMS[geom][0]))
+
+
+def _images(geom, coils, seed):
     g = torch.Generator(device="cpu").manual_seed(seed)
-    return torch.randn((coils,) + tuple(reversed(ND)), dtype=torch.complex64, generator=g).cuda()
+    return torch.randn(_image_shape(geom, coils), dtype=torch.complex64, generator=g).cuda()
 
 
 def _samples(coils, M, seed):
@@ -35,9 +46,9 @@ def _samples(coils, M, seed):
     return torch.randn((coils, M), dtype=torch.complex64, generator=g).cuda()
 
 
-def _per_coil(x, y):
+def _per_coil(geom, x, y):
     """Forward and adjoint of each coil alone on a fresh single-coil operator."""
-    A1 = _operator(1)
+    A1 = _operator(geom, 1)
     fw = [A1.plan.forward(x[c:c + 1].contiguous(),
                           torch.empty((1, A1.M), dtype=torch.complex64, device="cuda"), 1)
           for c in range(x.shape[0])]
@@ -52,25 +63,27 @@ def _fw(A, x):
                                                       device="cuda"), c)
 
 
-def _ad(A, y):
+def _ad(A, geom, y):
     c = y.shape[0]
-    return A.plan.adjoint(y.contiguous(), torch.empty((c,) + tuple(reversed(ND)),
-                                                      dtype=torch.complex64, device="cuda"), c)
+    return A.plan.adjoint(y.contiguous(), torch.empty(_image_shape(geom, c), dtype=torch.complex64,
+                                                      device="cuda"), c)
 
 
-def test_coil_count_changes_between_calls(gpu_lib):
-    A = _operator(COILS)
-    x, y = _images(COILS, 1), _samples(COILS, A.M, 2)
-    y_ref, x_ref = _per_coil(x, y)
+@pytest.mark.parametrize("geom", sorted(GEOMS))
+def test_coil_count_changes_between_calls(gpu_lib, geom):
+    A = _operator(geom, COILS)
+    x, y = _images(geom, COILS, 1), _samples(COILS, A.M, 2)
+    y_ref, x_ref = _per_coil(geom, x, y)
     for c in (COILS, 2, 5, 1, COILS, 3):
         assert rel_l2(_fw(A, x[:c]).cpu().numpy(), y_ref[:c].cpu().numpy()) < 1e-5, c
-        assert rel_l2(_ad(A, y[:c]).cpu().numpy(), x_ref[:c].cpu().numpy()) < 1e-5, c
+        assert rel_l2(_ad(A, geom, y[:c]).cpu().numpy(), x_ref[:c].cpu().numpy()) < 1e-5, c
 
 
-def test_graph_with_few_coils_replays_after_a_wider_call(gpu_lib):
-    A = _operator(COILS)
-    x, y = _images(COILS, 3), _samples(COILS, A.M, 4)
-    y_ref, x_ref = _per_coil(x, y)
+@pytest.mark.parametrize("geom", sorted(GEOMS))
+def test_graph_with_few_coils_replays_after_a_wider_call(gpu_lib, geom):
+    A = _operator(geom, COILS)
+    x, y = _images(geom, COILS, 3), _samples(COILS, A.M, 4)
+    y_ref, x_ref = _per_coil(geom, x, y)
     c = 2
     xs, ys = x[:c].contiguous(), y[:c].contiguous()
     yo = torch.empty((c, A.M), dtype=torch.complex64, device="cuda")
@@ -87,8 +100,8 @@ def test_graph_with_few_coils_replays_after_a_wider_call(gpu_lib):
         A.plan.forward(xs, yo, c)
         A.plan.adjoint(ys, xo, c)
     for _ in range(2):
-        _fw(A, x)                              # writes rows the graph reads as padding
-        _ad(A, y)
+        _fw(A, x)                              # 2-D: writes rows the graph reads as padding
+        _ad(A, geom, y)
         yo.zero_()
         xo.zero_()
         g.replay()
@@ -105,17 +118,18 @@ def test_graph_with_few_coils_replays_after_a_wider_call(gpu_lib):
     ((96, 10), (192, 20), "double"),
     ((512, 6), (1024, 12), "single"),
     ((1024, 6), (2048, 12), "single"),
+    ((16, 20, 12), (32, 40, 24), "single"),
+    ((12, 10, 14), (24, 20, 28), "double"),
 ])
 def test_row_lengths_match_oracle(gpu_lib, Nd, Kd, precision):
-    """The pruned row pass (N1 rows of each plane) and the column pass over
-    the row-interleaved grid, for short and long rows and both precisions,
-    against the oracle."""
+    """The pruned FFTs (2-D rows, 3-D z-planes) for short and long rows, 3-D
+    grids and both precisions, against the oracle."""
     from oracle import oracle as O
     from mrrt.nufft_gb300 import NufftBase
 
     rng = np.random.default_rng(7)
-    omega = rng.uniform(-np.pi, np.pi, (700, 2))
-    kw = dict(Nd=Nd, omega=omega, Jd=(6, 6), Kd=Kd, precision=precision)
+    omega = rng.uniform(-np.pi, np.pi, (700, len(Nd)))
+    kw = dict(Nd=Nd, omega=omega, Jd=(6,) * len(Nd), Kd=Kd, precision=precision)
     A = NufftBase(**kw)
     B = O.OracleNufft(**kw)
     cdt = np.complex64 if precision == "single" else np.complex128
