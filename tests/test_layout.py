@@ -140,3 +140,22 @@ def test_row_lengths_match_oracle(gpu_lib, Nd, Kd, precision):
     y = B.fft(x)
     assert rel_l2(A.fft(x), y) < tol
     assert rel_l2(A.adj(y), B.adj(y)) < tol
+
+
+@pytest.mark.parametrize("reps", [16, 17])
+def test_3d_pruning_limit_matches_oracle(gpu_lib, reps):
+    """3-D batches of up to 16 planes take the per-plane pruned FFT, larger
+    ones the full 3-D FFT; both against the oracle."""
+    from oracle import oracle as O
+    from mrrt.nufft_gb300 import NufftBase
+
+    Nd, Kd = (10, 12, 8), (20, 24, 16)
+    rng = np.random.default_rng(9)
+    omega = rng.uniform(-np.pi, np.pi, (500, 3))
+    kw = dict(Nd=Nd, omega=omega, Jd=(6, 6, 6), Kd=Kd)
+    A = NufftBase(max_coils=reps, **kw)
+    B = O.OracleNufft(**kw)
+    x = (rng.standard_normal(Nd + (reps,)) + 1j * rng.standard_normal(Nd + (reps,))).astype(np.complex64)
+    y = B.fft(x)
+    assert rel_l2(A.fft(x), y) < 1e-5
+    assert rel_l2(A.adj(y), B.adj(y)) < 1e-5
