@@ -48,3 +48,15 @@ def test_single_rank_needs_no_process_group():
 
     assert bench.max_over_ranks(3.0, 1, None) == 3.0
     assert bench.job_value(32, 1, 4.0) == pytest.approx(8000.0)
+
+
+def test_bench_parity_gate():
+    """bench.py stops before timing when the transform misses the metric's
+    accuracy bar; the oracle's own error figures are reported, not gated."""
+    import bench
+
+    bench.parity_gate({"fwd_rel_err_vs_oracle": 2.9e-7, "adj_rel_err_vs_fp64_oracle": 3.7e-5,
+                       "oracle_adj_rel_err_vs_fp64_oracle": 0.5})
+    for bad in (0.93, 2e-4, float("nan")):
+        with pytest.raises(SystemExit):
+            bench.parity_gate({"fwd_rel_err_vs_oracle": bad})
