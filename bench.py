@@ -91,14 +91,33 @@ def peaks():
 
 
 def clock_sampler_start(path):
+    """Start nvidia-smi sampling every 50 ms and return once it has written
+    its first line (at most 3 s), so that it is live when timing starts."""
     cmd = ["nvidia-smi", "--query-gpu=index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
            "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
            "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
-           "--format=csv,noheader,nounits", "-lms", "200"]
+           "--format=csv,noheader,nounits", "-lms", "50"]
     try:
-        return subprocess.Popen(cmd, stdout=open(path, "w"), stderr=subprocess.DEVNULL)
+        proc = subprocess.Popen(cmd, stdout=open(path, "w"), stderr=subprocess.DEVNULL)
     except (OSError, FileNotFoundError):
         return None
+    t_end = time.time() + 3.0
+    while time.time() < t_end and proc.poll() is None:
+        if os.path.exists(path) and os.path.getsize(path) > 0:
+            break
+        time.sleep(0.02)
+    return proc
+
+
+def load_tail(fn, seconds=0.3):
+    """Keep the timed workload running, untimed, while the clock sampler
+    takes a few more samples under the same load."""
+    import torch
+
+    t_end = time.time() + seconds
+    while time.time() < t_end:
+        fn()
+        torch.cuda.synchronize()
 
 
 def clock_sampler_stop(proc, path, device_index):
@@ -415,6 +434,8 @@ def run_ours(args, rank, world):
         gather()
     t_spread = time_events(spread, args.steps, flush) / args.steps
     t_gather = time_events(gather, args.steps, flush) / args.steps
+    if rank == 0:
+        load_tail(pair_graph)
     clocks = clock_sampler_stop(sampler, _clock_path(rank), dev.index) if rank == 0 else None
 
     # ---- plain per-call loop on the same GPU --------------------------------
@@ -605,6 +626,8 @@ def run_series(args, rank, world):
         gather()
     t_spread = time_events(spread, args.steps, flush) / args.steps
     t_gather = time_events(gather, args.steps, flush) / args.steps
+    if rank == 0:
+        load_tail(pair_graph)
     clocks = clock_sampler_stop(sampler, _clock_path(rank), dev.index) if rank == 0 else None
     del grid
 
