@@ -326,9 +326,9 @@ size_t list_bytes(const gbn_plan* P, int64_t len, bool with_ls) {
 
 // Gather tiling: start from a per-dimension default and halve the largest
 // edge until the staged tile + halo fits the shared-memory budget.
-// Spread tiling: a fixed number of register blocks per CTA (16 warps);
-// edges are multiples of the block edges and may exceed Kd (the cells past
-// Kd are never written).
+// Spread tiling: up to 8 register blocks per CTA, one warp each; edges are
+// multiples of the block edges and may exceed Kd (the cells past Kd are
+// never written).
 void choose_tiles(gbn_plan* P) {
     const gbn_geometry& G = P->geom;
     const int ndim = G.ndim;
