@@ -126,3 +126,70 @@ def test_reference_attributes_on_gpu_and_sparse_format(host_nufft):
     assert A.on_gpu is True
     kw = dict(c["kw"], mode="sparse")
     assert host_nufft(**kw).sparse_format == "CSC"
+
+
+class _HostIoPlan(_RecordingPlan):
+    """A recording plan whose host-buffer transforms compute a fixed linear
+    map in the device layouts: sample m of repetition r gets
+    (r + 1) * sum(image r), and every pixel of image r gets (r + 1) * sum(samples r)."""
+
+    def __init__(self, *a, **kw):
+        super().__init__(*a, **kw)
+        import torch
+
+        self.ctype = torch.complex64
+        self.calls = []
+
+    def forward_host(self, x, y, coils):
+        self.calls.append(("forward_host", tuple(x.shape), tuple(y.shape), coils, x.is_contiguous()))
+        xs = x.reshape(coils, -1).sum(dim=1)
+        for r in range(coils):
+            y[r].fill_((r + 1) * xs[r])
+        return y
+
+    def adjoint_host(self, y, x, coils):
+        self.calls.append(("adjoint_host", tuple(y.shape), tuple(x.shape), coils, y.is_contiguous()))
+        ys = y.reshape(coils, -1).sum(dim=1)
+        for r in range(coils):
+            x[r].fill_((r + 1) * ys[r])
+        return x
+
+
+@pytest.mark.parametrize("order", ["F", "C"])
+@pytest.mark.parametrize("reps", [1, 3])
+def test_numpy_calls_route_through_host_entry_points(monkeypatch, order, reps):
+    """NufftBase.fft/.adj on numpy arrays (on_gpu=False): one host-buffer call
+    each, with the image handed over as [reps][N1][N0] and the result returned
+    in the reference's layout for the order (reps last for 'F', first for
+    'C', squeezed when there is one)."""
+    import torch
+
+    from mrrt.nufft_gb300 import _nufft
+
+    monkeypatch.setattr(_nufft, "require_cuda", lambda: None)
+    monkeypatch.setattr(_nufft, "GpuPlan", _HostIoPlan)
+    monkeypatch.setattr(torch.cuda, "is_current_stream_capturing", lambda: False)
+    real_empty = torch.empty
+    monkeypatch.setattr(torch, "empty", lambda *a, pin_memory=False, **k: real_empty(*a, **k))
+
+    Nd = (6, 4)
+    omega = np.random.default_rng(1).uniform(-np.pi, np.pi, (10, 2))
+    A = _nufft.NufftBase(Nd, omega, Jd=(4, 4), Kd=(12, 8), order=order)
+    rng = np.random.default_rng(2)
+    shape = (Nd + (reps,)) if order == "F" else ((reps,) + Nd)
+    if reps == 1:
+        shape = Nd
+    x = (rng.standard_normal(shape) + 1j * rng.standard_normal(shape)).astype(np.complex64)
+    y = A.fft(x)
+    expect_y = (10,) if reps == 1 else ((10, reps) if order == "F" else (reps, 10))
+    assert isinstance(y, np.ndarray) and y.shape == expect_y and y.dtype == np.complex64
+    assert A.plan.calls[-1] == ("forward_host", (reps * 24,), (reps, 10), reps, True)
+    xr = x.reshape(Nd + (reps,)) if order == "F" else np.moveaxis(x.reshape((reps,) + Nd), 0, -1)
+    yr = y.reshape(10, reps) if order == "F" else np.moveaxis(y.reshape(reps, 10), 0, -1)
+    for r in range(reps):
+        np.testing.assert_allclose(yr[:, r], (r + 1) * xr[..., r].sum(), rtol=1e-5)
+    xa = A.adj(y)
+    assert xa.shape == x.shape and A.plan.calls[-1][0] == "adjoint_host"
+    xar = xa.reshape(Nd + (reps,)) if order == "F" else np.moveaxis(xa.reshape((reps,) + Nd), 0, -1)
+    for r in range(reps):
+        np.testing.assert_allclose(xar[..., r], (r + 1) * yr[:, r].sum(), rtol=1e-5)
