@@ -116,7 +116,9 @@ class NufftBase(object):
     """Non-uniform FFT operator (table-based interpolation) on the GPU.
 
     Parameters are those of the reference ``NufftBase``; see the module
-    docstring for the data conventions.  ``mode`` must be ``'table'``.
+    docstring for the data conventions.  ``mode`` is ``'table'`` or
+    ``'sparse'`` (the reference's exact Kaiser-Bessel interpolation weights,
+    applied by the same kernels).
 
     Extra keywords (not in the reference): ``max_coils`` -- the repetition
     count the tile plan is sized for (default 1).  Any batch size works; a
