@@ -1,8 +1,9 @@
 """mrrt.nufft_gb300 -- table-mode NUFFT for the NVIDIA GB300 (sm_103a).
 
 A drop-in for mritools/mrrt.nufft's ``NufftBase(Nd, omega, Jd, Kd,
-mode='table', precision=...)`` with ``.fft()`` / ``.adj()``, running on
-hand-written CUDA kernels behind the C ABI in ``include/gbnufft.h``.
+mode='table' | 'sparse', precision=...)`` with ``.fft()`` / ``.adj()``,
+running on hand-written CUDA kernels behind the C ABI in
+``include/gbnufft.h``.
 
 Exports mirror the reference package (mrrt/nufft/__init__.py:1-15) plus the
 batched torch operators and the autograd function.

@@ -1,8 +1,9 @@
 """Thin owner of a libgbnufft plan handle (host side of the C ABI).
 
 ``GpuPlan`` turns host-side plan math (tables, deapodisation, coordinates,
-sample phase) into a ``gbn_plan`` and calls the transforms on device
-pointers of torch tensors, on torch's current CUDA stream.  Everything here
+sample phase) into a ``gbn_plan`` and calls the transforms on torch's current
+CUDA stream: on CUDA tensors through the device entry points, and on CPU
+tensors (pageable or pinned) through the host-buffer ones.  Everything here
 is plumbing around the C ABI; the arithmetic runs in the CUDA kernels.
 """
 import ctypes
