@@ -768,9 +768,22 @@ def run_profile(args):
     from mrrt.nufft_gb300 import NufftBase
 
     w = WORKLOAD
-    if w["kind"] == "series":
-        raise SystemExit("--profile covers the single-operator workloads")
     C = w["coils"]
+    if w["kind"] == "series":
+        # the tile shapes the autotuner picks for this series (fixed here, so
+        # that no tuning launches enter a capture)
+        from mrrt.nufft_gb300.series import NufftSeries
+
+        S = NufftSeries(w["Nd"], _series_frames(w), Jd=w["Jd"], Kd=w["Kd"], Ld=w["L"], coils=C,
+                        tile=(32, 16), stile=(8, 8))
+        g = torch.Generator(device="cpu").manual_seed(0)
+        x_dev = torch.randn(S.image_shape, dtype=torch.complex64, generator=g).to(S.device)
+        for _ in range(args.warmup + args.steps):
+            S.adjoint(S.forward(x_dev))
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_case": w["name"], "coils": C, "samples": S.M_total,
+                          "stats": S.plan.stats()}))
+        return
     omega, x_f = build_inputs()
     A = NufftBase(Nd=w["Nd"], omega=omega, Jd=w["Jd"], Kd=w["Kd"], Ld=w["L"], precision="single",
                   on_gpu=True, max_coils=C)
