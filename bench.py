@@ -165,9 +165,21 @@ def time_events(fn, steps, flush=None):
     return sum(s.elapsed_time(e) for s, e in zip(starts, ends))
 
 
+# What each cpu_baseline kind runs.
+CPU_KIND_NOTE = {
+    "reference": "the reference's own table interpolation C (mrrt/nufft/_extensions/c/nufft_table.c, "
+                 "compiled on this host with its flags, -O2 -ffast-math -fopenmp)",
+    "port": "the oracle's C restatement of the reference table path",
+}
+
+
 def _cpu_operator(omega, w):
-    """The reference's CPU table operator where its package imports (this
-    container), else the oracle restatement (the GPU host); returns (op, kind)."""
+    """The CPU table operator timed as the reference: the reference package
+    itself where it imports (its sources present); else the reference's own
+    compiled interpolation kernels (oracle/_ref, rebuilt on this host from the
+    preprocessed unit) inside the oracle's restated pad / FFT / crop, which
+    is where the reference spends its time; else the oracle restatement.
+    Returns (op, kind)."""
     kw = dict(Nd=w["Nd"], omega=omega, Jd=w["Jd"], Kd=w["Kd"], Ld=w["L"], precision="single",
               mode="table")
     try:
@@ -177,8 +189,10 @@ def _cpu_operator(omega, w):
             return load_reference().NufftBase(**kw), "reference"
     except Exception:
         pass
-    from oracle import oracle
+    from oracle import oracle, refc
 
+    if refc.available():
+        return oracle.OracleNufft(interp=refc, **kw), "reference"
     return oracle.OracleNufft(**kw), "port"
 
 
@@ -206,8 +220,8 @@ def cpu_baseline(omega, x_f, min_seconds=10.0, max_reps=50):
         "unit": UNIT,
         "cores": os.cpu_count(),
         "kind": kind,
-        "sample": "%d x batched fwd+adj of %d of the workload's %d coils (%.2f s each)"
-                  % (reps, coils, w["coils"], per),
+        "sample": "%d x batched fwd+adj of %d of the workload's %d coils (%.2f s each); %s"
+                  % (reps, coils, w["coils"], per, CPU_KIND_NOTE[kind]),
         "seconds_per_pair_batch": per,
     }
 
@@ -277,7 +291,7 @@ def run_reference(args, rank):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "complex64",
         "data": "synthetic", "config": config_dict(),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": os.cpu_count(), "kind": kind,
-                         "sample": sample},
+                         "sample": sample + "; " + CPU_KIND_NOTE[kind]},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)

@@ -157,7 +157,11 @@ int gbn_interp_forward(gbn_plan* plan, const void* grid, void* y, int coils,
 int gbn_interp_adjoint(gbn_plan* plan, const void* y, void* grid, int coils,
                        void* stream);
 
-/* Capacity of the fixed scratch array behind gbn_interp_adjoint_noalloc. */
+/* Capacity of the fixed scratch array behind gbn_interp_adjoint_noalloc.
+ * Under lazy module loading (CUDA_MODULE_LOADING=LAZY, the CUDA default) the
+ * array is reserved on a device only once a process first calls the no-alloc
+ * entry point there; with CUDA_MODULE_LOADING=EAGER every process that loads
+ * libgbnufft reserves it on each device it initialises.                     */
 #define GBN_NOALLOC_SCRATCH_BYTES (64u * 1024u * 1024u)
 
 /* Same result as gbn_interp_adjoint, for callers that must not allocate
@@ -171,9 +175,10 @@ int gbn_interp_adjoint(gbn_plan* plan, const void* y, void* grid, int coils,
  *   - Limit: the partial sums of one call must fit GBN_NOALLOC_SCRATCH_BYTES
  *     (64 MiB); a larger request returns GBN_ERR_TOOLARGE before anything
  *     is launched.  Fewer coils per call, or gbn_interp_adjoint, fit it.
- *   - The first call on a device looks up that array's address (which can
- *     also load the module holding it); make that first call before any
- *     stream capture.
+ *   - Every call looks up the array's address on the current device (no
+ *     allocation; it stays right after a device reset).  The first call on
+ *     a device can also load the module holding the array: make that first
+ *     call before any stream capture.
  *   - Every plan on a device shares the one array: calls whose kernels can
  *     overlap in time (unordered streams, or several host threads) race on
  *     it and corrupt each other's results.  Order them on one stream or
@@ -239,6 +244,14 @@ const char* gbn_last_error(void);
 
 /* Library version string. */
 const char* gbn_version(void);
+
+/* Testing hook, no counterpart in the reference: host-side fault injection
+ * for the allocation-failure paths.  After this call, `after` more device
+ * allocations made by the library succeed and the next one fails as if
+ * cudaMalloc had reported cudaErrorMemoryAllocation (nothing is requested
+ * from the device for it); the call that needed it returns GBN_ERR_NOMEM.
+ * A negative value turns the injection off.  Process-wide.                 */
+int gbn_debug_fail_alloc(long long after);
 
 #ifdef __cplusplus
 }

@@ -86,6 +86,7 @@ SIGNATURES = {
     "gbn_plan_stats": [_VP, ctypes.POINTER(_I64)],
     "gbn_last_error": [],
     "gbn_version": [],
+    "gbn_debug_fail_alloc": [ctypes.c_longlong],
 }
 
 _lib = None

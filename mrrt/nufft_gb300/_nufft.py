@@ -132,6 +132,14 @@ class NufftBase(object):
                  preplan_cufft=True, order="F", verbose=False, on_gpu=False, max_coils=1,
                  tile=None, stile=None):
         require_cuda()
+        # the constructor's arguments, kept so that a pickled operator is
+        # rebuilt (replanned on the GPU) on load; the reference's operator is
+        # picklable (mrrt/nufft/_nufft.py:405-407)
+        self._init_args = dict(
+            Nd=Nd, omega=np.array(_to_numpy(omega), copy=True), Jd=Jd, Kd=Kd, precision=precision,
+            mode=mode, Ld=Ld, ortho=ortho, n_shift=n_shift, phasing=phasing,
+            adjoint_scalefactor=adjoint_scalefactor, preplan_cufft=preplan_cufft, order=order,
+            verbose=verbose, on_gpu=on_gpu, max_coils=max_coils, tile=tile, stile=stile)
         self.verbose = verbose
         self.order = order
         if order not in ("F", "C"):
@@ -510,4 +518,11 @@ class NufftBase(object):
         return self._device_out(g, reps, self.__Kd)
 
     def __getstate__(self):
-        raise TypeError("NufftBase holds GPU state; rebuild it from (Nd, omega, ...) instead of pickling")
+        """Pickle the constructor's arguments (not the GPU state); loading
+        rebuilds the plan on the current CUDA device."""
+        state = dict(self._init_args)
+        state["on_gpu"] = self.on_gpu
+        return state
+
+    def __setstate__(self, state):
+        self.__init__(**state)

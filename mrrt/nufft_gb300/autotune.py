@@ -8,11 +8,13 @@ real plan (sorted lists for that tiling) and is timed with CUDA events on
 the current stream after a warm-up launch, median of ``reps`` launches.
 Results are cached in memory, and in a JSON file when ``cache_path`` (or the
 ``GBNUFFT_TUNE_CACHE`` environment variable) names one, keyed by geometry,
-sample counts, coil count and precision.
+per-frame sample counts, a SHA-256 digest of the trajectory itself, coil
+count and precision.
 
 The reference has no tile shapes to tune (its CPU kernels loop over samples,
 its CuPy kernels launch one thread per sample).
 """
+import hashlib
 import json
 import os
 import threading
@@ -40,9 +42,22 @@ def candidate_tiles(ndim):
             [(8, 8, 2), (16, 8, 1), (8, 4, 4), (16, 4, 2), (4, 4, 8)])
 
 
-def _key(kind, Nd, Kd, Jd, counts, coils, precision):
-    return "%s|%s|%s|%s|%d|%d|%d|%s" % (kind, tuple(Nd), tuple(Kd), tuple(Jd), len(counts),
-                                         int(np.sum(counts)), int(coils), precision)
+def trajectory_digest(omegas):
+    """SHA-256 of every frame's coordinates (as float64, row-major), so that
+    two trajectories with the same sample counts get different cache keys."""
+    h = hashlib.sha256()
+    for om in omegas:
+        a = om.detach().cpu().numpy() if isinstance(om, torch.Tensor) else np.asarray(om)
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        h.update(np.asarray(a.shape, dtype=np.int64).tobytes())
+        h.update(a.tobytes())
+    return h.hexdigest()[:32]
+
+
+def _key(kind, Nd, Kd, Jd, counts, coils, precision, digest):
+    return "%s|%s|%s|%s|%s|%d|%s|%s" % (kind, tuple(Nd), tuple(Kd), tuple(Jd),
+                                       ",".join(str(int(c)) for c in counts), int(coils), precision,
+                                       digest)
 
 
 def _load(path):
@@ -112,7 +127,7 @@ def tune_series(Nd, omegas, Jd=6, Kd=None, Ld=1024, coils=1, precision="single",
     Jd = (Jd,) * ndim if np.isscalar(Jd) else tuple(Jd)
     Kd = tuple(Kd) if Kd is not None else tuple(int(1.5 * n) for n in Nd)
     counts = [int(np.asarray(o).shape[0]) for o in omegas]
-    key = _key("series", Nd, Kd, Jd, counts, coils, precision)
+    key = _key("series", Nd, Kd, Jd, counts, coils, precision, trajectory_digest(omegas))
     path = cache_path or os.environ.get("GBNUFFT_TUNE_CACHE")
     with _lock:
         if key in _cache:

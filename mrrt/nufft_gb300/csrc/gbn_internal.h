@@ -205,7 +205,7 @@ int spread_threads(int ndim, const int* T);
 cudaError_t ensure_dynamic_smem(const void* kernel, size_t bytes);
 
 // Address and size of the fixed no-alloc scratch array on the current device
-// (gbn_noalloc.cu); looked up on the first request per device.
+// (gbn_noalloc.cu); looked up on every request.
 cudaError_t noalloc_scratch(void** ptr, size_t* bytes);
 
 cudaError_t launch_dtft(bool adjoint, int ndim, const int* Nd, const double* n_shift,

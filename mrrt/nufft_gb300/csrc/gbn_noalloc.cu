@@ -9,12 +9,13 @@
 // module image, so the CUDA driver reserves it when the module loads and no
 // allocator is ever called for it.
 //
-// The array lives in its own translation unit so that the module holding it
-// (and its 64 MiB) is only loaded by processes that use the no-alloc entry
-// point.
+// The array lives in its own translation unit.  Under lazy module loading
+// (CUDA_MODULE_LOADING=LAZY, the default since CUDA 12.2) the module holding
+// it, and its 64 MiB, is loaded on a device only when a process first uses
+// the no-alloc entry point there.  With CUDA_MODULE_LOADING=EAGER every
+// process that loads libgbnufft reserves the 64 MiB on each device it
+// initialises.
 #include <cuda_runtime.h>
-
-#include <mutex>
 
 #include "../../../include/gbnufft.h"
 #include "gbn_internal.h"
@@ -25,29 +26,16 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[GBN_NOALLOC_SCR
 
 namespace gbn {
 
-namespace {
-constexpr int NOALLOC_MAX_DEVICES = 64;
-std::mutex g_noalloc_mu;
-void* g_noalloc_addr[NOALLOC_MAX_DEVICES] = {};
-}  // namespace
-
-// Device address of the array on the current device.  The first request on
-// a device looks it up (with that device current) and caches it; later
-// requests only read the cache.
+// Device address of the array on the current device, looked up on every
+// call.  The lookup allocates nothing once the module is loaded, and a
+// fresh lookup stays right after cudaDeviceReset or a re-created primary
+// context, which may load the module (and the array) at another address.
 cudaError_t noalloc_scratch(void** ptr, size_t* bytes) {
-    int dev = -1;
-    cudaError_t e = cudaGetDevice(&dev);
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess) return e;
-    if (dev < 0 || dev >= NOALLOC_MAX_DEVICES) return cudaErrorInvalidDevice;
-    std::lock_guard<std::mutex> lk(g_noalloc_mu);
-    if (!g_noalloc_addr[dev]) {
-        void* p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess) return e;
-        if (!p) return cudaErrorInvalidSymbol;
-        g_noalloc_addr[dev] = p;
-    }
-    *ptr = g_noalloc_addr[dev];
+    if (!p) return cudaErrorInvalidSymbol;
+    *ptr = p;
     *bytes = sizeof(g_noalloc_scratch);
     return cudaSuccess;
 }

@@ -8,11 +8,13 @@
 // global atomics, mrrt/nufft/cuda/jinja/table_2d_adjoint.jinja).
 #include <cuda_runtime.h>
 #include <cufft.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <atomic>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -58,7 +60,9 @@ int fail(int code, const std::string& msg) {
 }
 
 int cuda_fail(cudaError_t e, const char* where) {
-    return fail(GBN_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+    // an allocation that failed is reported as such, whatever the call site
+    const int code = e == cudaErrorMemoryAllocation ? GBN_ERR_NOMEM : GBN_ERR_CUDA;
+    return fail(code, std::string(where) + ": " + cudaGetErrorString(e));
 }
 
 int cufft_fail(cufftResult r, const char* where) {
@@ -94,6 +98,19 @@ Lanes make_lanes(int ndim, int coils) {
     return ln;
 }
 
+// Host-side fault injection for tests (gbn_debug_fail_alloc): the number of
+// further device allocations that succeed before one fails, or -1 (off).
+std::atomic<long long> g_fail_alloc_after{-1};
+
+// True when the injection says this allocation is the one that fails.
+bool injected_alloc_failure() {
+    long long n = g_fail_alloc_after.load();
+    while (n >= 0) {
+        if (g_fail_alloc_after.compare_exchange_weak(n, n - 1)) return n == 0;
+    }
+    return false;
+}
+
 struct DevBuf {
     void* p = nullptr;
     size_t bytes = 0;
@@ -105,6 +122,7 @@ struct DevBuf {
         p = nullptr;
         bytes = 0;
         if (b == 0) return cudaSuccess;
+        if (injected_alloc_failure()) return cudaErrorMemoryAllocation;
         cudaError_t e = cudaMalloc(&p, b);
         if (e == cudaSuccess) bytes = b;
         return e;
@@ -186,6 +204,16 @@ struct gbn_plan {
 };
 
 namespace {
+
+// NVTX range over a host scope: the stages of a transform appear by name
+// (and nest) in a profiler's timeline.  Header-only NVTX v3: without a tool
+// attached a push/pop is a branch on a null function pointer.
+struct NvtxRange {
+    explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange&) = delete;
+    NvtxRange& operator=(const NvtxRange&) = delete;
+};
 
 struct DeviceGuard {
     int prev = -1;
@@ -858,7 +886,7 @@ int run_spread(gbn_plan* P, const void* y, void* grid, int coils, bool phases, c
 // The spread of run_spread with the split-tile partial sums kept in the
 // fixed no-alloc array instead of the plan's scratch buffer.  Nothing here
 // allocates: the size check happens before any launch, and the array's
-// address comes from a per-device lookup done once.
+// address comes from a lookup on the current device at every call.
 template <typename R>
 int run_spread_noalloc(gbn_plan* P, const void* y, void* grid, int coils, cudaStream_t s) {
     typedef typename Cx<R>::T C;
@@ -934,8 +962,15 @@ int run_forward(gbn_plan* P, const void* x, void* y, int coils, cudaStream_t s, 
     pp.maps = reinterpret_cast<const typename Cx<R>::T*>(maps);
     pp.coils = coils;
     internal_layout(P, P->F * coils, pp);
-    GBN_CUDA(launch_pad<R>(pp, s), "pad launch");
-    if ((rc = fft_forward(P, P->F * coils, s))) return rc;
+    {
+        NvtxRange r("gbn forward: pad");
+        GBN_CUDA(launch_pad<R>(pp, s), "pad launch");
+    }
+    {
+        NvtxRange r("gbn forward: fft");
+        if ((rc = fft_forward(P, P->F * coils, s))) return rc;
+    }
+    NvtxRange r("gbn forward: gather");
     return run_gather<R>(P, P->grid.p, y, coils, true, s);
 }
 
@@ -946,9 +981,15 @@ int run_adjoint(gbn_plan* P, const void* y, void* x, int coils, cudaStream_t s, 
     int rc = ensure_buffers(P, coils);
     if (rc) return rc;
     if (!P->grid.p) return fail(GBN_ERR_NOMEM, "grid buffer missing");
-    rc = run_spread<R>(P, y, P->grid.p, coils, true, s);
-    if (rc) return rc;
-    if ((rc = fft_inverse(P, P->F * coils, s))) return rc;
+    {
+        NvtxRange r("gbn adjoint: spread");
+        rc = run_spread<R>(P, y, P->grid.p, coils, true, s);
+        if (rc) return rc;
+    }
+    {
+        NvtxRange r("gbn adjoint: fft");
+        if ((rc = fft_inverse(P, P->F * coils, s))) return rc;
+    }
     const gbn_geometry& G = P->geom;
     CropParams<R> cp;
     std::memset(&cp, 0, sizeof(cp));
@@ -967,6 +1008,7 @@ int run_adjoint(gbn_plan* P, const void* y, void* x, int coils, cudaStream_t s, 
     cp.maps = reinterpret_cast<const typename Cx<R>::T*>(maps);
     cp.coils = coils;
     internal_layout(P, P->F * coils, cp);
+    NvtxRange r("gbn adjoint: crop");
     GBN_CUDA(launch_crop<R>(cp, s), "crop launch");
     return GBN_OK;
 }
@@ -1531,6 +1573,11 @@ int gbn_plan_stats(const gbn_plan* P, int64_t* o) {
 }
 
 const char* gbn_last_error(void) { return g_last_error.c_str(); }
+
+int gbn_debug_fail_alloc(long long after) {
+    g_fail_alloc_after.store(after < 0 ? -1 : after);
+    return GBN_OK;
+}
 
 const char* gbn_version(void) { return "gbnufft 0.1.0 (sm_103a)"; }
 

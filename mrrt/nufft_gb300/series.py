@@ -115,8 +115,21 @@ class NufftSeries(object):
         return y
 
     def adjoint(self, y, x=None, coils=None):
-        """Frame-major samples -> images ``[F, coils, *reversed(Nd)]``."""
-        c = self.coils if coils is None else coils
+        """Frame-major samples -> images ``[F, coils, *reversed(Nd)]``.  The
+        coil count comes from ``coils``, else from ``x``, else from the size
+        of ``y`` (which must hold ``coils * M_total`` samples)."""
+        if coils is None:
+            if x is not None:
+                coils = x.shape[1]
+            elif y.numel() % self.M_total == 0 and self.M_total > 0:
+                coils = y.numel() // self.M_total
+            else:
+                raise ValueError("y holds %d samples, not a multiple of the series' %d"
+                                 % (y.numel(), self.M_total))
+        c = int(coils)
+        if y.numel() != c * self.M_total:
+            raise ValueError("y holds %d samples but %d coils x %d samples were expected"
+                             % (y.numel(), c, self.M_total))
         x = self.empty_images(c) if x is None else x
         self.plan.adjoint(y, x, c)
         return x

@@ -306,7 +306,13 @@ class OracleNufft:
     (mrrt/nufft/_nufft.py:216-360, 425-482), CPU only."""
 
     def __init__(self, Nd, omega, Jd=4, Kd=None, precision="single", mode="table", Ld=1024,
-                 ortho=False, n_shift=None, phasing="real", adjoint_scalefactor=1.0, order="F"):
+                 ortho=False, n_shift=None, phasing="real", adjoint_scalefactor=1.0, order="F",
+                 interp=None):
+        # interp: a module with interp_forward / interp_adjoint of this
+        # module's signatures (``oracle.refc`` runs the reference's own
+        # compiled kernels); None uses the C restatement
+        self._interp_fwd = interp.interp_forward if interp is not None else interp_forward
+        self._interp_adj = interp.interp_adjoint if interp is not None else interp_adjoint
         if np.isscalar(Nd):
             Nd = (Nd,)
         self.Nd = _as_tuple(Nd)
@@ -433,7 +439,7 @@ class OracleNufft:
         if self.ortho:
             xk /= self.scale_ortho
         if self.mode == "table":
-            y = interp_forward(xk, self.h, self.Jd, self.Ld, self.tm, self.Kd)
+            y = self._interp_fwd(xk, self.h, self.Jd, self.Ld, self.tm, self.Kd)
             if self.phase_shift is not None:
                 y *= self.phase_shift[:, None]
             y = y.astype(xk.dtype, copy=False)
@@ -459,7 +465,7 @@ class OracleNufft:
         if self.mode == "table":
             if self.phase_shift is not None:
                 xk *= self.phase_shift.conj()[:, None]
-            xk_all = interp_adjoint(xk, self.h, self.Jd, self.Ld, self.tm, self.Kd)
+            xk_all = self._interp_adj(xk, self.h, self.Jd, self.Ld, self.tm, self.Kd)
         else:
             xk_all = self.p.conj().T * xk
         xk_all = xk_all.reshape(Kd + (n_reps,), order="F")

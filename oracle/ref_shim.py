@@ -35,7 +35,22 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(HERE)
-DEFAULT_REF = os.environ.get("MRRT_REFERENCE_ROOT", "/root/reference")
+
+
+def _reference_root():
+    """The reference checkout: MRRT_REFERENCE_ROOT, else the one the build
+    recorded in oracle/_ref/REF_ROOT when it compiled the reference there."""
+    root = os.environ.get("MRRT_REFERENCE_ROOT")
+    if root:
+        return root
+    marker = os.path.join(HERE, "_ref", "REF_ROOT")
+    if os.path.exists(marker):
+        with open(marker) as f:
+            return f.read().strip() or None
+    return None
+
+
+DEFAULT_REF = _reference_root()
 
 
 def _standin_utils():
@@ -101,6 +116,8 @@ def _standin_utils():
 
 
 def reference_available(ref_root=DEFAULT_REF):
+    if not ref_root:
+        return False
     ext = os.path.join(HERE, "_ref", "_nufft_table" + sysconfig.get_config_var("EXT_SUFFIX"))
     return os.path.isdir(os.path.join(ref_root, "mrrt", "nufft")) and os.path.exists(ext)
 

@@ -101,7 +101,13 @@ def test_autotune_cache_round_trip(tmp_path):
     from mrrt.nufft_gb300 import autotune
 
     path = str(tmp_path / "tune.json")
-    key = autotune._key("series", (64, 64), (128, 128), (6, 6), [10, 20], 4, "single")
+    rng = np.random.default_rng(0)
+    om_a = [rng.uniform(-3, 3, (10, 2)), rng.uniform(-3, 3, (20, 2))]
+    om_b = [om_a[0], om_a[1] + 1e-3]   # same counts, another trajectory
+    da, db = autotune.trajectory_digest(om_a), autotune.trajectory_digest(om_b)
+    assert da != db and da == autotune.trajectory_digest([o.copy() for o in om_a])
+    key = autotune._key("series", (64, 64), (128, 128), (6, 6), [10, 20], 4, "single", da)
+    assert key != autotune._key("series", (64, 64), (128, 128), (6, 6), [10, 20], 4, "single", db)
     assert autotune._load(path) == {}
     autotune._store(path, key, {"tile": [32, 16], "stile": [8, 8], "report": {}})
     autotune._store(path, key + "x", {"tile": [16, 8], "stile": [16, 8], "report": {}})

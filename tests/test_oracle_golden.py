@@ -96,6 +96,36 @@ def test_oracle_interp_bit_identical_to_reference_c():
     assert rel_l2(g_or, g_ref) < 1e-6
 
 
+@pytest.mark.skipif(not __import__("oracle.refc").refc.available(), reason="oracle/_ref not built")
+@pytest.mark.parametrize("ndim", [1, 2, 3])
+def test_reference_c_library_matches_oracle_restatement(ndim):
+    """The reference's own compiled kernels (oracle/_ref, built from its
+    sources or from the preprocessed unit on a machine without them) and the
+    oracle's C restatement: forward bit for bit, adjoint to rounding, on
+    coordinates that wrap around both ends of the grid."""
+    from oracle import refc
+
+    rng = np.random.default_rng(11 + ndim)
+    K = (40, 36, 20)[:ndim]
+    N = (20, 18, 10)[:ndim]
+    M = 700
+    tm = np.stack([rng.uniform(-2 * k, 3 * k, M) for k in K], -1).astype(np.float32)
+    h = [np.asarray(O.table_make1(N[d], 6, K[d], 256, "real")[0]).astype(np.float32) for d in range(ndim)]
+    ck = (rng.standard_normal(K + (3,)) + 1j * rng.standard_normal(K + (3,))).astype(np.complex64)
+    y_ref = refc.interp_forward(ck, h, (6,) * ndim, 256, tm, K)
+    y_or = O.interp_forward(ck, h, (6,) * ndim, 256, tm, K)
+    assert np.array_equal(y_ref, y_or)
+    fm = (rng.standard_normal((M, 3)) + 1j * rng.standard_normal((M, 3))).astype(np.complex64)
+    g_ref = refc.interp_adjoint(fm, h, (6,) * ndim, 256, tm, K)
+    g_or = O.interp_adjoint(fm, h, (6,) * ndim, 256, tm, K)
+    assert rel_l2(g_or, g_ref) < 1e-6
+    A = O.OracleNufft(N, tm[:, :ndim] * (2 * np.pi / np.asarray(K)), Jd=6, Kd=K, Ld=256, interp=refc)
+    B = O.OracleNufft(N, tm[:, :ndim] * (2 * np.pi / np.asarray(K)), Jd=6, Kd=K, Ld=256)
+    x = (rng.standard_normal(N) + 1j * rng.standard_normal(N)).astype(np.complex64)
+    assert rel_l2(A.fft(x), B.fft(x)) < 1e-6
+    assert rel_l2(A.adj(fm[:, 0]), B.adj(fm[:, 0])) < 1e-6
+
+
 def test_exported_kaiser_bessel_helpers_match_reference():
     """kaiser_bessel, kaiser_bessel_ft and BeattyKernel (exported like the
     reference's, mrrt/nufft/__init__.py) against values the reference

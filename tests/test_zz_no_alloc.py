@@ -19,13 +19,13 @@ NOALLOC_CAP = 64 * 1024 * 1024   # GBN_NOALLOC_SCRATCH_BYTES
 TOL = 1e-6                       # same kernels, same part order: results agree to rounding
 
 
-def _plan(tm, N, K, J, L=512, max_coils=1):
+def _plan(tm, N, K, J, L=512, max_coils=1, rdt=np.float32):
     from mrrt.nufft_gb300._kernels import kernel_table
     from mrrt.nufft_gb300._plan import GpuPlan
 
-    h = [kernel_table(N[d], J[d], K[d], L, "real", np.float32) for d in range(len(N))]
-    return GpuPlan(N, K, J, L, np.float32, h, None, np.ones(int(np.prod(N)), np.float32),
-                   np.ascontiguousarray(tm, dtype=np.float32), None, max_coils=max_coils)
+    h = [kernel_table(N[d], J[d], K[d], L, "real", rdt) for d in range(len(N))]
+    return GpuPlan(N, K, J, L, rdt, h, None, np.ones(int(np.prod(N)), rdt),
+                   np.ascontiguousarray(tm, dtype=rdt), None, max_coils=max_coils)
 
 
 def _call(P, name, y, grid, coils):
@@ -37,7 +37,7 @@ def _call(P, name, y, grid, coils):
 def _noalloc(P, y, coils):
     from mrrt.nufft_gb300 import _lib
 
-    grid = torch.empty((coils, P.Kprod), dtype=torch.complex64, device="cuda")
+    grid = torch.empty((coils, P.Kprod), dtype=y.dtype, device="cuda")
     _lib.check(_call(P, "gbn_interp_adjoint_noalloc", y, grid, coils))
     return grid
 
@@ -45,14 +45,38 @@ def _noalloc(P, y, coils):
 def _regular(P, y, coils):
     from mrrt.nufft_gb300 import _lib
 
-    grid = torch.empty((coils, P.Kprod), dtype=torch.complex64, device="cuda")
+    grid = torch.empty((coils, P.Kprod), dtype=y.dtype, device="cuda")
     _lib.check(_call(P, "gbn_interp_adjoint", y, grid, coils))
     return grid
 
 
-def _samples(coils, M, seed):
+def _samples(coils, M, seed, dtype=torch.complex64):
     g = torch.Generator(device="cuda").manual_seed(seed)
-    return torch.randn((coils, M), dtype=torch.complex64, device="cuda", generator=g)
+    return torch.randn((coils, M), dtype=dtype, device="cuda", generator=g)
+
+
+@pytest.mark.parametrize("case", ["2d-double", "3d-single"])
+def test_noalloc_double_and_3d_match_interp_adjoint(gpu_lib, case):
+    """The double-precision instantiation (2-D radial, 4 coils) and a 3-D
+    geometry whose centre tiles are split (radial spokes through one point,
+    3 coils): two consecutive no-alloc calls each match gbn_interp_adjoint."""
+    from mrrt.nufft_gb300.trajectories import kooshball_3d, radial_2d
+
+    if case == "2d-double":
+        N, K, J, coils, rdt, ct = (64, 64), (128, 128), (6, 6), 4, np.float64, torch.complex128
+        tm = radial_2d(160, 128, golden=True) / (2 * np.pi / 128.0)
+    else:
+        N, K, J, coils, rdt, ct = (24, 24, 24), (48, 48, 48), (6, 6, 6), 3, np.float32, torch.complex64
+        tm = kooshball_3d(2000, 48) / (2 * np.pi / 48.0)
+    P = _plan(tm, N, K, J, max_coils=coils, rdt=rdt)
+    assert P.stats()["split_tiles"] > 0, "the case must exercise the split-tile scratch"
+    tol = 1e-12 if rdt == np.float64 else TOL
+    for seed in (5, 6):
+        y = _samples(coils, P.M_total, seed, ct)
+        g = _noalloc(P, y, coils)
+        r = _regular(P, y, coils)
+        torch.cuda.synchronize()
+        assert rel_l2(g.cpu().numpy(), r.cpu().numpy()) < tol
 
 
 def test_noalloc_matches_interp_adjoint_two_calls(gpu_lib):
