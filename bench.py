@@ -53,6 +53,10 @@ WORKLOADS = {
     # the 3-D kernels on a smaller volume (inputs still larger than L2), for profiler captures
     "3d-kooshball-96": dict(name="3d-kooshball-96", kind="koosh3d", Nd=(96, 96, 96), Kd=(192, 192, 192),
                             Jd=(6, 6, 6), L=1024, spokes=6000, readout=192, coils=8),
+    # differentiable NUFFT: loss ||A(x; omega) - y||^2, gradients in x and omega, the trajectory
+    # moved every step (device re-binning)
+    "2d-spiral-grad": dict(name="2d-spiral-grad", kind="grad2d", Nd=(256, 256), Kd=(512, 512), Jd=(6, 6),
+                           L=1024, interleaves=16, samples=4096, coils=1),
     # uneven dynamic series: every frame and coil in one launch per stage, CUDA graph, autotuned tiles
     "series-2d": dict(name="series-2d", kind="series", Nd=(192, 192), Kd=(384, 384), Jd=(6, 6),
                       L=1024, frames=64, readout=384, min_spokes=13, max_spokes=89, seed=4, coils=8),
@@ -254,6 +258,10 @@ def run_reference(args, rank):
     if rank != 0:
         return
     w = WORKLOAD
+    if w["kind"] == "grad2d":
+        print(json.dumps({"impl": "reference", "unavailable": "the reference has no autograd: no gradient "
+                          "with respect to the image or the trajectory to time"}), flush=True)
+        return
     if w["kind"] == "series":
         frames = _series_frames(w)[:4]
         ops, kind = [], "port"
@@ -327,6 +335,9 @@ def config_dict(extra=None):
     elif w["kind"] == "koosh3d":
         cfg["trajectory"] = "kooshball %d spokes x %d on a Fibonacci sphere" % (w["spokes"], w["readout"])
         cfg["samples"] = w["spokes"] * w["readout"]
+    elif w["kind"] == "grad2d":
+        cfg["trajectory"] = "variable-density spiral %d x %d" % (w["interleaves"], w["samples"])
+        cfg["samples"] = w["interleaves"] * w["samples"]
     else:
         cfg["trajectory"] = ("%d frames, U{%d..%d} golden-angle spokes (seed %d) x %d"
                              % (w["frames"], w["min_spokes"], w["max_spokes"], w["seed"], w["readout"]))
@@ -359,6 +370,8 @@ def run_ours(args, rank, world):
 
     if WORKLOAD["kind"] == "series":
         return run_series(args, rank, world)
+    if WORKLOAD["kind"] == "grad2d":
+        return run_grad(args, rank, world)
     dev = torch.device("cuda", torch.cuda.current_device())
     w = WORKLOAD
     C = w["coils"]
@@ -531,6 +544,125 @@ def run_ours(args, rank, world):
         "plan": stats,
     }
     print(json.dumps(line), flush=True)
+
+
+def run_grad(args, rank, world):
+    """Differentiable NUFFT step: y_hat = A(x; omega), loss = ||y_hat - y||^2,
+    backward to x (the adjoint transform) and to omega (the derivative-table
+    gather K5), with the trajectory moved every step (as an optimiser of the
+    trajectory would) and its samples re-binned on the device.  Timed: the
+    whole step, the re-bin alone, and K5 alone (CUDA events)."""
+    import torch
+
+    from mrrt.nufft_gb300.autograd import NufftOperator
+    from mrrt.nufft_gb300.trajectories import complex_image, spiral_2d
+
+    w = WORKLOAD
+    dev = torch.device("cuda", torch.cuda.current_device())
+    C, Nd, Kd = w["coils"], w["Nd"], w["Kd"]
+    om0 = spiral_2d(w["interleaves"], w["samples"])
+    M = om0.shape[0]
+    op = NufftOperator(Nd, om0, Jd=w["Jd"], Kd=Kd, Ld=w["L"], max_coils=C)
+    x_true = torch.from_numpy(np.stack([complex_image(Nd, seed=1 + c) for c in range(C)])).to(dev)
+    g = torch.Generator(device="cpu").manual_seed(0)
+    with torch.no_grad():
+        y0 = op.forward(x_true)
+        noise = torch.randn(y0.shape, dtype=torch.complex64, generator=g).to(dev)
+        y = y0 + 0.01 * y0.abs().pow(2).mean().sqrt() * noise
+    y64 = y.to(torch.complex128)
+    x = torch.randn((C,) + Nd, dtype=torch.complex64, generator=g).to(dev).requires_grad_(True)
+    om_base = torch.from_numpy(om0.astype(np.float32)).to(dev)
+    # two trajectories alternate, so every step re-bins
+    oms = [om_base, om_base + 1e-3]
+
+    def step(k):
+        om = oms[k % 2].clone().requires_grad_(True)
+        loss = (op.forward(x, om).to(torch.complex128) - y64).abs().pow(2).sum()
+        loss.backward()
+        return loss, om.grad
+
+    # parity (untimed): the omega gradient along a random +-1 direction
+    # against central differences of the loss (steps 1e-3 and 5e-4 rad,
+    # Richardson-extrapolated: the 1e-3 difference alone carries an O(eps^2)
+    # truncation of about 1%)
+    loss0, gom = step(0)
+    v = torch.from_numpy(np.random.default_rng(9).choice([-1.0, 1.0], (M, 2))).to(dev, torch.float32)
+
+    def loss_at(o):
+        with torch.no_grad():
+            return float((op.forward(x, o).to(torch.complex128) - y64).abs().pow(2).sum())
+
+    def central(h):
+        return (loss_at(oms[0] + h * v) - loss_at(oms[0] - h * v)) / (2 * h)
+
+    fd1, fd2 = central(1e-3), central(5e-4)
+    rich = (4 * fd2 - fd1) / 3
+    an = float((gom.double() * v.double()).sum())
+    parity = {"omega_grad_rel_err_vs_richardson_central_difference": abs(rich - an) / abs(an),
+              "omega_grad_rel_err_vs_central_difference_1e-3": abs(fd1 - an) / abs(an)}
+    if parity["omega_grad_rel_err_vs_richardson_central_difference"] > 2e-3:
+        print("bench.py: omega gradient off: %s" % json.dumps(parity), file=sys.stderr, flush=True)
+        raise SystemExit(1)
+
+    for k in range(args.warmup):
+        step(k)
+    torch.cuda.synchronize()
+    flush_buf = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    sampler = clock_sampler_start(_clock_path(rank)) if rank == 0 else None
+    t_steps = []
+    for k in range(args.steps):
+        flush_buf.fill_(1.0)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        step(k)
+        torch.cuda.synchronize()
+        t_steps.append(time.perf_counter() - t0)
+    # re-bin alone (device binning of a changed trajectory)
+    t_bin = []
+    for k in range(args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        op.set_omega(oms[(k + 1) % 2])
+        torch.cuda.synchronize()
+        t_bin.append(time.perf_counter() - t0)
+    # K5 alone: the derivative-table gather on the forward grid
+    op.set_omega(oms[0])
+    xp = op._image_to_plan(x.detach())
+    scratch = torch.empty((C, M), dtype=torch.complex64, device=dev)
+    op.plan.forward(xp, scratch, C)
+    gy = torch.randn((C, M), dtype=torch.complex64, generator=g).to(dev)
+    gtm = torch.empty((M, 2), dtype=torch.float32, device=dev)
+    grid_ptr = op.plan.forward_grid(C)
+
+    def k5():
+        op.plan.grad_tm(grid_ptr, gy, op.phase_shift, gtm, C)
+
+    for _ in range(3):
+        k5()
+    t_k5 = time_events(k5, args.steps) / args.steps
+    clocks = clock_sampler_stop(sampler, _clock_path(rank), dev.index) if rank == 0 else None
+    if rank != 0:
+        return
+    t_step = float(np.median(t_steps))
+    Kp = int(np.prod(Kd))
+    B_k5 = C * Kp * 8 + C * M * 8 + M * 2 * 4 + M * 2 * 4
+    hbm, peak_kind = peaks()
+    achieved = B_k5 / (t_k5 * 1e-3) / 1e9
+    line = {
+        "metric": "differentiable NUFFT steps/s (forward, image and omega gradients, device re-bin)",
+        "value": 1.0 / t_step, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * t_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "complex64", "data": "synthetic", "config": config_dict(),
+        "rebin_ms": 1e3 * float(np.median(t_bin)),
+        "k5": {"kernel_ms": t_k5, "algorithmic_bytes": B_k5,
+               "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "peak_kind": peak_kind,
+                            "unit": "GB/s", "frac": achieved / hbm}},
+        "loss": float(loss0.item()), "parity": parity, "clocks": clocks,
+        "timing": "host clock around each step with torch.cuda.synchronize (the step is a chain of "
+                  "launches with two small device-to-host reads in the re-bin); K5 by CUDA events",
+    }
+    print(json.dumps(line), flush=True)
+
 
 
 def _series_frames(w):

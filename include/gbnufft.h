@@ -98,6 +98,20 @@ int gbn_plan_create(gbn_plan** plan, const gbn_geometry* geom,
 int gbn_plan_set_points(gbn_plan* plan, const void* tm,
                         const void* sample_phase);
 
+/* gbn_plan_set_points with DEVICE arrays: tm [M_total][ndim] and
+ * sample_phase [M_total] (or NULL) in device memory, plan precision.  The
+ * tile lists are built on the device by a sort of the samples (stable, so
+ * the spread's summation order, hence its result, is the same in every
+ * run); the coordinates never pass through host memory.  The call waits
+ * for work already queued on the device, and for two 4-to-16-byte counts it
+ * reads back on `stream` (to size the lists and launches), then returns with
+ * the rest queued on `stream`.  Invalid coordinates (non-finite, |tm| >
+ * 2^22) return GBN_ERR_INVALID and keep the previous lists.  Replaces the
+ * host-side tm = omega / gamma recomputation of the reference
+ * (mrrt/nufft/_nufft.py:338-342) when a trajectory is optimised on the GPU. */
+int gbn_plan_set_points_device(gbn_plan* plan, const void* tm,
+                               const void* sample_phase, void* stream);
+
 int gbn_plan_destroy(gbn_plan* plan);
 
 /* Forward NUFFT, image -> samples, `coils` coils per frame.

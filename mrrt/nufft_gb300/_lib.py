@@ -65,6 +65,7 @@ SIGNATURES = {
     "gbn_plan_create": [ctypes.POINTER(_VP), ctypes.POINTER(GbnGeometry), ctypes.POINTER(_VP),
                         ctypes.POINTER(_VP), _VP, ctypes.POINTER(_I64), _VP, _VP, _I],
     "gbn_plan_set_points": [_VP, _VP, _VP],
+    "gbn_plan_set_points_device": [_VP, _VP, _VP, _VP],
     "gbn_plan_destroy": [_VP],
     "gbn_forward": [_VP, _VP, _VP, _I, _VP],
     "gbn_adjoint": [_VP, _VP, _VP, _I, _VP],

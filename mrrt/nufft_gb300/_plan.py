@@ -253,6 +253,26 @@ class GpuPlan:
         with torch.cuda.device(self.device):
             _lib.check(self.lib.gbn_plan_set_points(self.handle, _vp(tm), _vp(ph)))
 
+    def set_points_device(self, tm, sample_phase=None):
+        """Replace the coordinates from device tensors (``tm`` [M_total, ndim]
+        in the plan's real dtype, ``sample_phase`` [M_total] complex or None):
+        the tile lists are rebuilt by kernels on the plan's device, on the
+        current stream."""
+        rt = torch.float32 if self.rdt == np.float32 else torch.float64
+        tm = tm.to(device=self.device, dtype=rt).contiguous()
+        if tm.numel() != self.M_total * self.ndim:
+            raise ValueError("set_points keeps the sample count; got %d coordinates, expected %d"
+                             % (tm.numel(), self.M_total * self.ndim))
+        ph = None
+        if sample_phase is not None:
+            ph = sample_phase.to(device=self.device, dtype=self.ctype).contiguous()
+            if ph.numel() != self.M_total:
+                raise ValueError("sample_phase needs %d values" % self.M_total)
+        with torch.cuda.device(self.device):
+            _lib.check(self.lib.gbn_plan_set_points_device(
+                self.handle, ctypes.c_void_p(tm.data_ptr()),
+                ctypes.c_void_p(ph.data_ptr()) if ph is not None else None, _stream()))
+
     def stats(self):
         out = (ctypes.c_int64 * 8)()
         _lib.check(self.lib.gbn_plan_stats(self.handle, out))

@@ -22,7 +22,10 @@ computes x = A(omega)^H y, both through ``torch.autograd.Function``s:
 
 The reference has no autograd; its forward / adjoint definitions are
 mrrt/nufft/_nufft.py:1275-1397 and 1459-1578.  When omega changes between
-calls the plan's sample lists are rebuilt (host sort + upload).
+calls the plan's sample lists are rebuilt: for a CUDA tensor omega by the
+device binning (``gbn_plan_set_points_device``: tm = omega / gamma and the
+sample phase computed on the GPU, the samples sorted by tile there, the
+coordinates never copied to the host); for a host array by the host planner.
 """
 import numpy as np
 import torch
@@ -62,14 +65,31 @@ class NufftOperator(object):
         self.phase_shift = [float(self.shift_vec[d]) * float(self.gamma[d]) for d in range(self.ndim)]
         self.plan.set_dtables(b.kernel_deriv_tables())
         self._omega = om.copy()
+        self._omega_t = torch.as_tensor(om, device=self.device)   # the plan's current trajectory
+        self._gamma_t = torch.tensor(self.gamma, dtype=torch.float64, device=self.device)
+        self._shift_t = torch.as_tensor(self.shift_vec, device=self.device)
 
     # ----------------------------------------------------------- trajectory
     def set_omega(self, omega):
         """Move the samples to ``omega`` ([M, ndim], radians); rebuilds the
-        plan's tile lists if the coordinates changed."""
+        plan's tile lists if the coordinates changed.  A CUDA tensor stays on
+        the device (device binning); a host array goes through the host
+        planner."""
+        if isinstance(omega, torch.Tensor) and omega.is_cuda:
+            om = omega.detach().to(device=self.device, dtype=self.rtdtype).reshape(self.M, self.ndim)
+            if om.data_ptr() == self._omega_t.data_ptr() or torch.equal(om, self._omega_t):
+                return
+            # tm = omega / gamma (in double, rounded to the operator's dtype) and
+            # exp(i omega . (n_shift - n_mid)), as the host path computes them
+            tm = (om.to(torch.float64) / self._gamma_t).to(self.rtdtype).contiguous()
+            phase = torch.exp(1j * (om @ self._shift_t)).to(self.tdtype)
+            self.plan.set_points_device(tm, phase)
+            self._omega_t = om.clone()
+            self._omega = None
+            return
         om = omega.detach().cpu().numpy() if isinstance(omega, torch.Tensor) else np.asarray(omega)
         om = np.ascontiguousarray(om, dtype=self.rdt).reshape(self.M, self.ndim)
-        if np.array_equal(om, self._omega):
+        if self._omega is not None and np.array_equal(om, self._omega):
             return
         tm = np.zeros_like(om)
         for d in range(self.ndim):
@@ -77,6 +97,7 @@ class NufftOperator(object):
         phase = np.exp(1j * np.dot(om, self.shift_vec)).astype(self.cdt, copy=False)
         self.plan.set_points(tm, phase)
         self._omega = om.copy()
+        self._omega_t = torch.as_tensor(om, device=self.device)
 
     # ---------------------------------------------------------- layout glue
     def _image_to_plan(self, x):
@@ -127,7 +148,7 @@ class NufftOperator(object):
 
 def _omega_arg(omega, op):
     if omega is None:
-        return torch.as_tensor(op._omega, device=op.device)
+        return op._omega_t
     return omega
 
 

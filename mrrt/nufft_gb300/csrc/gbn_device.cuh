@@ -14,6 +14,8 @@ __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
 __device__ __forceinline__ double2 cmul(double2 a, double2 b) {
     return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
 // a * conj(b)
 __device__ __forceinline__ float2 cmulc(float2 a, float2 b) {
     return make_float2(a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y);

@@ -11,8 +11,11 @@
 // the same sample points as h_d, linearly interpolated the same way.  With
 // torch's convention for the incoming gradient gy = dL/dRe(y) + i dL/dIm(y),
 //   dL/dt_d = sum_c Re(conj(gy[m,c]) dy[m,c]/dt_d).
-// One thread per sample; coils are summed inside the thread.  The kernel has
-// no counterpart in the reference, which has no autograd.
+// One thread per sample (samples in gather-list order, so neighbouring
+// threads read neighbouring grid taps); coils are summed inside the thread.
+// phase_before is separable, so it is folded into the per-axis coefficients
+// (J sincos per axis per sample instead of one per tap per coil).  The
+// kernel has no counterpart in the reference, which has no autograd.
 #include <cuda_runtime.h>
 
 #include "gbn_device.cuh"
@@ -26,93 +29,86 @@ __global__ void __launch_bounds__(128) grad_kernel(const GradParams<R> p) {
     const Geom<R>& g = p.g;
     const int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (m >= p.M) return;
-    R t[3];
-    int kf[3];
+    // Per axis and tap: the table coefficient and its derivative, each
+    // times that axis's factor of phase_before.  phase_before(k) =
+    // exp(i sum_d c_d k_d) is a product over axes, so the phases cost
+    // J sincos per axis per sample instead of one per tap per coil.
+    C cc[NDIM][JMAX], dd[NDIM][JMAX];
+    int kf[3] = {0, 0, 0};
 #pragma unroll
     for (int d = 0; d < NDIM; ++d) {
-        t[d] = p.t[d][m];
-        kf[d] = first_tap(t[d], g.J[d]);
-    }
-    R c[NDIM][JMAX], dc[NDIM][JMAX];
-#pragma unroll
-    for (int d = 0; d < NDIM; ++d) {
+        const R t = p.t[d][m];
+        kf[d] = first_tap(t, g.J[d]);
 #pragma unroll
         for (int j = 0; j < JMAX; ++j) {
-            c[d][j] = (R)0;
-            dc[d][j] = (R)0;
+            cc[d][j] = cmake<R>((R)0, (R)0);
+            dd[d][j] = cmake<R>((R)0, (R)0);
             if (j < g.J[d]) {
-                R ci;
-                table_coef<R, false>(g, d, t[d], kf[d] + j, c[d][j], ci);
-                const R pp = (t[d] - (R)(kf[d] + j)) * (R)g.L;
+                R c, ci;
+                table_coef<R, false>(g, d, t, kf[d] + j, c, ci);
+                const R pp = (t - (R)(kf[d] + j)) * (R)g.L;
                 const R nf = floor(pp);
                 const int n = min(max((int)nf + g.ncenter[d], -2), g.J[d] * g.L + 1);
-                const R alf = pp - nf;
-                dc[d][j] = lerp_rn(alf, __ldg(p.dh[d] + n), __ldg(p.dh[d] + n + 1));
+                const R dc = lerp_rn(pp - nf, __ldg(p.dh[d] + n), __ldg(p.dh[d] + n + 1));
+                R sn = (R)0, cs = (R)1;
+                if (p.apply_pb) sincos_r(mul_rn(g.pbc[d], (R)wrapk(kf[d] + j, g.K[d])), &sn, &cs);
+                cc[d][j] = cmake<R>(c * cs, c * sn);
+                dd[d][j] = cmake<R>(dc * cs, dc * sn);
             }
         }
     }
     const C ph = p.ph ? p.ph[m] : cmake<R>((R)1, (R)0);
+    const R inv_scale = (R)1 / p.grid_scale;
     R out[3] = {0, 0, 0};
-    for (int cc = 0; cc < p.coils; ++cc) {
-        const C* gb = p.grid + (int64_t)cc * g.gsp;
+    constexpr int D1 = NDIM > 1 ? 1 : 0, D2 = NDIM > 2 ? 2 : 0;
+    for (int co = 0; co < p.coils; ++co) {
+        const C* gb = p.grid + (int64_t)co * g.gsp;
         C G = cmake<R>(0, 0), D[3] = {cmake<R>(0, 0), cmake<R>(0, 0), cmake<R>(0, 0)};
 #pragma unroll 1
-        for (int j2 = 0; j2 < (NDIM > 2 ? JMAX : 1); ++j2) {
-            if (NDIM > 2 && j2 >= g.J[2]) continue;
+        for (int j2 = 0; j2 < (NDIM > 2 ? g.J[D2] : 1); ++j2) {
+            C G1 = cmake<R>(0, 0), D10 = cmake<R>(0, 0), D11 = cmake<R>(0, 0);
+            const int64_t o2 = NDIM > 2 ? (int64_t)wrapk(kf[D2] + j2, g.K[D2]) * g.gs2 : 0;
 #pragma unroll 1
-            for (int j1 = 0; j1 < (NDIM > 1 ? JMAX : 1); ++j1) {
-                if (NDIM > 1 && j1 >= g.J[1]) continue;
-                C rc = cmake<R>(0, 0), rd = cmake<R>(0, 0);
+            for (int j1 = 0; j1 < (NDIM > 1 ? g.J[D1] : 1); ++j1) {
+                const int64_t o1 = NDIM > 1 ? (int64_t)wrapk(kf[D1] + j1, g.K[D1]) * g.gs1 : 0;
+                C r = cmake<R>(0, 0), rd = cmake<R>(0, 0);
 #pragma unroll
                 for (int j0 = 0; j0 < JMAX; ++j0) {
                     if (j0 >= g.J[0]) continue;
-                    int k[3] = {0, 0, 0};
-                    k[0] = wrapk(kf[0] + j0, g.K[0]);
-                    if (NDIM > 1) k[1] = wrapk(kf[NDIM > 1 ? 1 : 0] + j1, g.K[1]);
-                    if (NDIM > 2) k[2] = wrapk(kf[NDIM > 2 ? 2 : 0] + j2, g.K[2]);
-                    const int64_t off = k[0] + (int64_t)k[1] * g.gs1 + (int64_t)k[2] * g.gs2;
-                    C v = gb[off];
-                    if (p.apply_pb) v = cmul(v, phase_before(g, k));
-                    v.x /= p.grid_scale;
-                    v.y /= p.grid_scale;
-                    rc.x += c[0][j0] * v.x;
-                    rc.y += c[0][j0] * v.y;
-                    rd.x += dc[0][j0] * v.x;
-                    rd.y += dc[0][j0] * v.y;
+                    const C v = gb[wrapk(kf[0] + j0, g.K[0]) + o1 + o2];
+                    r = cadd(r, cmul(cc[0][j0], v));
+                    rd = cadd(rd, cmul(dd[0][j0], v));
                 }
-                R w1 = (R)1, dw1 = (R)0;
                 if (NDIM > 1) {
-                    w1 = c[NDIM > 1 ? 1 : 0][j1];
-                    dw1 = dc[NDIM > 1 ? 1 : 0][j1];
-                }
-                R w2 = (R)1, dw2 = (R)0;
-                if (NDIM > 2) {
-                    w2 = c[NDIM > 2 ? 2 : 0][j2];
-                    dw2 = dc[NDIM > 2 ? 2 : 0][j2];
-                }
-                const R a = w1 * w2;
-                G.x += a * rc.x;
-                G.y += a * rc.y;
-                D[0].x += a * rd.x;
-                D[0].y += a * rd.y;
-                if (NDIM > 1) {
-                    D[1].x += dw1 * w2 * rc.x;
-                    D[1].y += dw1 * w2 * rc.y;
-                }
-                if (NDIM > 2) {
-                    D[2].x += w1 * dw2 * rc.x;
-                    D[2].y += w1 * dw2 * rc.y;
+                    const C w1 = cc[D1][j1], dw1 = dd[D1][j1];
+                    G1 = cadd(G1, cmul(w1, r));
+                    D10 = cadd(D10, cmul(w1, rd));
+                    D11 = cadd(D11, cmul(dw1, r));
+                } else {
+                    G1 = r;
+                    D10 = rd;
                 }
             }
+            if (NDIM > 2) {
+                const C w2 = cc[D2][j2], dw2 = dd[D2][j2];
+                G = cadd(G, cmul(w2, G1));
+                D[0] = cadd(D[0], cmul(w2, D10));
+                D[1] = cadd(D[1], cmul(w2, D11));
+                D[2] = cadd(D[2], cmul(dw2, G1));
+            } else {
+                G = G1;
+                D[0] = D10;
+                D[1] = D11;
+            }
         }
-        const C gy = p.gy[(int64_t)cc * p.M + p.idx[m]];
+        const C gy = p.gy[(int64_t)co * p.M + p.idx[m]];
         const C y = cmul(ph, G);
         // Re(conj(gy) * i * y) = Re(gy) * (-Im y) + Im(gy) * Re(y)
-        const R ry = -gy.x * y.y + gy.y * y.x;
+        const R ry = (-gy.x * y.y + gy.y * y.x) * inv_scale;
 #pragma unroll
         for (int d = 0; d < NDIM; ++d) {
-            const C dd = cmul(ph, D[d]);
-            out[d] += gy.x * dd.x + gy.y * dd.y + p.phase_shift[d] * ry;
+            const C dv = cmul(ph, D[d]);
+            out[d] += (gy.x * dv.x + gy.y * dv.y) * inv_scale + p.phase_shift[d] * ry;
         }
     }
 #pragma unroll

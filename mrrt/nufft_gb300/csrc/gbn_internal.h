@@ -184,6 +184,81 @@ struct GradParams {
     R* gtm;                         // [M][ndim] out
 };
 
+// Device binning (gbn_bin.cu): per-sample pass over coordinates tm
+// ([M][ndim], plan precision, device) for the plan's tilings.
+template <typename R>
+struct BinParams {
+    int ndim, F;
+    int K[3], J[3], Tg[3], ntg[3], Ts[3], nts[3];
+    int ntiles_g, ntiles_s;        // per frame
+    double tm_limit;               // |tm| bound (larger or non-finite: err)
+    int64_t M;
+    const R* tm;
+    const int64_t* foff;           // device frame offsets [F+1]
+    int* err;                      // set to 1 on an invalid coordinate
+    unsigned* gkey;                // [M] gather bin (frame * ntiles_g + tile)
+    unsigned* gval;                // [M] sample index (sort payload)
+    int* ecount;                   // [M] spread entries of each sample
+    const int* eoff;               // [M] exclusive scan of ecount (emit pass)
+    unsigned* skey;                // [entries] spread bin
+    unsigned* sval;                // [entries] entry index (sort payload)
+    int* em;                       // [entries] sample index
+    short4* els;                   // [entries] window start in tile coordinates
+};
+
+// Work items from per-bin counts (starts = exclusive scans of the counts).
+struct ItemParams {
+    int nbins_g, nbins_s, ntiles_g, ntiles_s;
+    int gchunk, schunk;
+    const int* gcnt;
+    const int* gstart;
+    const int* scnt;
+    const int* sstart;
+    int* gparts;                   // parts pass: gather items per bin
+    int* sparts;                   //   spread items per bin
+    int* rslots;                   //   scratch slots per bin (parts of split tiles)
+    int* rflag;                    //   1 for a split tile
+    const int* goff;               // items pass: scans of the above
+    const int* soff;
+    const int* slotoff;
+    const int* roff;
+    int4* gitems;
+    unsigned* gsize;               // sort key: chunk - count (heaviest first)
+    unsigned* gorder;
+    int4* sitems;
+    int2* sslot;
+    unsigned* ssize;
+    unsigned* sorder;
+    int4* rtiles;
+};
+
+// List packing: position i of a sorted list takes sample em[order[i]] (or
+// order[i] itself when em is null, the gather list).
+template <typename R>
+struct PackParams {
+    int ndim, F;
+    int64_t len;
+    const unsigned* order;
+    const int* em;
+    const short4* els;
+    const R* tm;
+    const typename Cx<R>::T* ph;
+    const int64_t* foff;
+    short4* ls_out;
+    typename Cx<R>::T* ph_out;
+    R* t_out[3];
+    int* idx_out;
+};
+
+template <typename R> cudaError_t launch_bin_count(const BinParams<R>& p, cudaStream_t s);
+template <typename R> cudaError_t launch_bin_emit(const BinParams<R>& p, cudaStream_t s);
+cudaError_t launch_bin_hist(const unsigned* keys, int64_t n, int* counts, cudaStream_t s);
+cudaError_t launch_bin_parts(const ItemParams& p, cudaStream_t s);
+cudaError_t launch_bin_items(const ItemParams& p, cudaStream_t s);
+cudaError_t launch_permute_int4(const int4* in, const unsigned* order, int64_t n, int4* out, cudaStream_t s);
+cudaError_t launch_permute_int2(const int2* in, const unsigned* order, int64_t n, int2* out, cudaStream_t s);
+template <typename R> cudaError_t launch_bin_pack(const PackParams<R>& p, cudaStream_t s);
+
 template <typename R> cudaError_t launch_gather(const GatherParams<R>& p, cudaStream_t s);
 template <typename R> cudaError_t launch_spread(const SpreadParams<R>& p, cudaStream_t s);
 template <typename R> cudaError_t launch_reduce(const ReduceParams<R>& p, cudaStream_t s);

@@ -21,6 +21,7 @@
 
 #include "../../../include/gbnufft.h"
 #include "gbn_internal.h"
+#include "gbn_sort.cuh"
 
 using namespace gbn;
 
@@ -180,6 +181,7 @@ struct gbn_plan {
     DevBuf gcoef, scoef;  // precomputed coefficients in gather / spread list order
     bool coefs = false;   // gcoef / scoef hold the current lists' coefficients
     DevBuf glist, gitems;
+    DevBuf bin_ws, bin_ws2;   // device binning workspaces (grown on demand)
     DevBuf slist, sitems, sparts, rtiles;
     int n_gitems = 0, n_sitems = 0, n_rtiles = 0, n_slots = 0;
     int64_t glen = 0, slen = 0;
@@ -1202,7 +1204,7 @@ int validate(const gbn_geometry* g) {
 // sparse-mode weights when set, else from the tables unless the geometry
 // asks for table interpolation inside the kernels (GBN_FLAG_TABLE_ONLY).
 template <typename R>
-int fill_coefs(gbn_plan* P) {
+int fill_coefs(gbn_plan* P, cudaStream_t stream = 0, bool sync = true) {
     P->coefs = false;
     const gbn_geometry& G = P->geom;
     if (!P->weights.p && (G.flags & GBN_FLAG_TABLE_ONLY)) {
@@ -1243,9 +1245,9 @@ int fill_coefs(gbn_plan* P) {
         c.out_i = P->cx ? c.out_r + (size_t)len * jsum : nullptr;
         c.jsum = jsum;
         c.cx = P->cx ? 1 : 0;
-        GBN_CUDA(launch_coef<R>(c, 0), "coefficient launch");
+        GBN_CUDA(launch_coef<R>(c, stream), "coefficient launch");
     }
-    GBN_CUDA(cudaDeviceSynchronize(), "coefficient precompute");
+    if (sync) GBN_CUDA(cudaDeviceSynchronize(), "coefficient precompute");
     P->coefs = true;
     return GBN_OK;
 }
@@ -1257,6 +1259,258 @@ int plan_points(gbn_plan* P, const void* tm, const void* phase) {
     int rc = build_lists<R>(P, reinterpret_cast<const R*>(tm), reinterpret_cast<const R*>(phase));
     if (rc) return rc;
     return fill_coefs<R>(P);
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Device binning: the lists of build_lists built by kernels (gbn_bin.cu,
+// gbn_sort.cu) from device coordinates.  Two small reads come back to the
+// host (the entry count, to size the spread list, and the item counts, to
+// size the launches); the coordinates and lists stay on the device.
+namespace {
+
+// Bump allocation of 256-byte aligned pieces of a workspace; with a null
+// base it only sums the sizes (sizing pass).
+struct Bump {
+    char* base;
+    size_t off = 0;
+    explicit Bump(void* b) : base(reinterpret_cast<char*>(b)) {}
+    template <typename T>
+    T* take(int64_t n) {
+        T* p = base ? reinterpret_cast<T*>(base + off) : nullptr;
+        off += ((size_t)std::max<int64_t>(n, 1) * sizeof(T) + 255) & ~(size_t)255;
+        return p;
+    }
+};
+
+int bits_for(int64_t n) {
+    int b = 0;
+    while ((int64_t(1) << b) < n) ++b;
+    return std::max(b, 1);
+}
+
+template <typename R>
+int device_build_lists(gbn_plan* P, const R* tm, const typename Cx<R>::T* ph, cudaStream_t s) {
+    typedef typename Cx<R>::T C;
+    const gbn_geometry& G = P->geom;
+    const int ndim = G.ndim;
+    const int64_t M = P->M_total;
+    const int ntg = P->ntiles_g, nts = P->ntiles_s;
+    const int64_t nbg = (int64_t)P->F * ntg, nbs = (int64_t)P->F * nts;
+    int64_t bound = M;
+    for (int d = 0; d < ndim; ++d) bound *= G.Jd[d];
+    if (bound > INT32_MAX || nbg > INT32_MAX / 2 || nbs > INT32_MAX / 2)
+        return fail(GBN_ERR_TOOLARGE, "device binning: more than 2^31 possible list entries");
+    const int SCH = ndim == 3 ? 2 * SPREAD_CHUNK : SPREAD_CHUNK;
+
+    // ---- phase A: per-sample tiles and entry counts ----------------------
+    const int64_t nmax = std::max<int64_t>(std::max<int64_t>(M, nbg), nbs);
+    int *err, *tot, *ecount, *eoff;
+    unsigned *gkey, *gval;
+    void* scan_tmp;
+    auto layout_a = [&](Bump& b) {
+        err = b.take<int>(16);
+        tot = b.take<int>(16);
+        gkey = b.take<unsigned>(M);
+        gval = b.take<unsigned>(M);
+        ecount = b.take<int>(M);
+        eoff = b.take<int>(M);
+        scan_tmp = b.take<char>((int64_t)scan_temp_bytes(nmax));
+    };
+    {
+        Bump sz(nullptr);
+        layout_a(sz);
+        if (sz.off > P->bin_ws.bytes) {
+            cudaError_t e = P->bin_ws.alloc(sz.off);
+            if (e != cudaSuccess) return cuda_fail(e, "binning workspace");
+        }
+        Bump b(P->bin_ws.p);
+        layout_a(b);
+    }
+    BinParams<R> bp;
+    std::memset(&bp, 0, sizeof(bp));
+    bp.ndim = ndim;
+    bp.F = P->F;
+    for (int d = 0; d < 3; ++d) {
+        bp.K[d] = d < ndim ? G.Kd[d] : 1;
+        bp.J[d] = d < ndim ? G.Jd[d] : 1;
+        bp.Tg[d] = P->Tg[d];
+        bp.ntg[d] = P->ntg[d];
+        bp.Ts[d] = P->Ts[d];
+        bp.nts[d] = P->nts[d];
+    }
+    bp.ntiles_g = ntg;
+    bp.ntiles_s = nts;
+    bp.tm_limit = TM_LIMIT;
+    bp.M = M;
+    bp.tm = tm;
+    bp.foff = reinterpret_cast<const int64_t*>(P->dfoff.p);
+    bp.err = err;
+    bp.gkey = gkey;
+    bp.gval = gval;
+    bp.ecount = ecount;
+    bp.eoff = eoff;
+    GBN_CUDA(cudaMemsetAsync(err, 0, 32 * sizeof(int), s), "binning reset");
+    GBN_CUDA(launch_bin_count<R>(bp, s), "bin count launch");
+    GBN_CUDA(exclusive_scan(ecount, eoff, M, tot, scan_tmp, s), "entry scan");
+    int hA[2] = {0, 0};
+    GBN_CUDA(cudaMemcpyAsync(&hA[0], err, sizeof(int), cudaMemcpyDeviceToHost, s), "binning readback");
+    GBN_CUDA(cudaMemcpyAsync(&hA[1], tot, sizeof(int), cudaMemcpyDeviceToHost, s), "binning readback");
+    GBN_CUDA(cudaStreamSynchronize(s), "binning readback");
+    if (hA[0]) return fail(GBN_ERR_INVALID, "sample coordinate is not finite or |tm| > 2^22");
+    const int64_t slen = hA[1];
+
+    // ---- phase B: spread entries, sorts, bins, items ---------------------
+    const int64_t nsort = std::max<int64_t>(std::max<int64_t>(M, slen), nbs);
+    const int64_t nitem_max = nbg + M / GATHER_CHUNK + 1 + nbs + slen / SCH + 1;
+    unsigned *skey, *sval, *gsize, *gorder, *ssize, *sorder;
+    int *em, *cg, *cs, *sg, *ss, *gp, *sp, *rs, *rf, *go, *so, *slo, *ro;
+    short4* els;
+    int4 *gi_tmp, *si_tmp;
+    int2* sl_tmp;
+    void* rtmp;
+    auto layout_b = [&](Bump& b) {
+        skey = b.take<unsigned>(slen);
+        sval = b.take<unsigned>(slen);
+        em = b.take<int>(slen);
+        els = b.take<short4>(slen);
+        cg = b.take<int>(nbg);
+        cs = b.take<int>(nbs);
+        sg = b.take<int>(nbg);
+        ss = b.take<int>(nbs);
+        gp = b.take<int>(nbg);
+        sp = b.take<int>(nbs);
+        rs = b.take<int>(nbs);
+        rf = b.take<int>(nbs);
+        go = b.take<int>(nbg);
+        so = b.take<int>(nbs);
+        slo = b.take<int>(nbs);
+        ro = b.take<int>(nbs);
+        gi_tmp = b.take<int4>(nitem_max);
+        si_tmp = b.take<int4>(nitem_max);
+        sl_tmp = b.take<int2>(nitem_max);
+        gsize = b.take<unsigned>(nitem_max);
+        gorder = b.take<unsigned>(nitem_max);
+        ssize = b.take<unsigned>(nitem_max);
+        sorder = b.take<unsigned>(nitem_max);
+        rtmp = b.take<char>((int64_t)radix_temp_bytes(nsort));
+    };
+    {
+        Bump sz(nullptr);
+        layout_b(sz);
+        if (sz.off > P->bin_ws2.bytes) {
+            cudaError_t e = P->bin_ws2.alloc(sz.off);
+            if (e != cudaSuccess) return cuda_fail(e, "binning workspace");
+        }
+        Bump b(P->bin_ws2.p);
+        layout_b(b);
+    }
+    bp.skey = skey;
+    bp.sval = sval;
+    bp.em = em;
+    bp.els = els;
+    GBN_CUDA(launch_bin_emit<R>(bp, s), "bin emit launch");
+    GBN_CUDA(radix_sort_pairs(gkey, gval, M, bits_for(nbg), rtmp, s), "gather sort");
+    GBN_CUDA(radix_sort_pairs(skey, sval, slen, bits_for(nbs), rtmp, s), "spread sort");
+    GBN_CUDA(cudaMemsetAsync(cg, 0, sizeof(int) * nbg, s), "bin count reset");
+    GBN_CUDA(cudaMemsetAsync(cs, 0, sizeof(int) * nbs, s), "bin count reset");
+    GBN_CUDA(launch_bin_hist(gkey, M, cg, s), "gather bin counts");
+    GBN_CUDA(launch_bin_hist(skey, slen, cs, s), "spread bin counts");
+    GBN_CUDA(exclusive_scan(cg, sg, nbg, nullptr, scan_tmp, s), "gather bin scan");
+    GBN_CUDA(exclusive_scan(cs, ss, nbs, nullptr, scan_tmp, s), "spread bin scan");
+    ItemParams ip;
+    std::memset(&ip, 0, sizeof(ip));
+    ip.nbins_g = (int)nbg;
+    ip.nbins_s = (int)nbs;
+    ip.ntiles_g = ntg;
+    ip.ntiles_s = nts;
+    ip.gchunk = GATHER_CHUNK;
+    ip.schunk = SCH;
+    ip.gcnt = cg;
+    ip.gstart = sg;
+    ip.scnt = cs;
+    ip.sstart = ss;
+    ip.gparts = gp;
+    ip.sparts = sp;
+    ip.rslots = rs;
+    ip.rflag = rf;
+    GBN_CUDA(launch_bin_parts(ip, s), "bin parts launch");
+    GBN_CUDA(exclusive_scan(gp, go, nbg, tot + 1, scan_tmp, s), "gather item scan");
+    GBN_CUDA(exclusive_scan(sp, so, nbs, tot + 2, scan_tmp, s), "spread item scan");
+    GBN_CUDA(exclusive_scan(rs, slo, nbs, tot + 3, scan_tmp, s), "slot scan");
+    GBN_CUDA(exclusive_scan(rf, ro, nbs, tot + 4, scan_tmp, s), "split tile scan");
+    int hB[4] = {0, 0, 0, 0};
+    GBN_CUDA(cudaMemcpyAsync(hB, tot + 1, 4 * sizeof(int), cudaMemcpyDeviceToHost, s), "binning readback");
+    GBN_CUDA(cudaStreamSynchronize(s), "binning readback");
+    const int n_gi = hB[0], n_si = hB[1], n_slots = hB[2], n_rt = hB[3];
+    auto ensure = [&](DevBuf& b, size_t bytes, const char* what) -> int {
+        bytes = std::max<size_t>(bytes, 16);
+        if (b.bytes < bytes) {
+            cudaError_t e = b.alloc(bytes);
+            if (e != cudaSuccess) return cuda_fail(e, what);
+        }
+        return GBN_OK;
+    };
+    int rc;
+    if ((rc = ensure(P->gitems, (size_t)n_gi * sizeof(int4), "item allocation"))) return rc;
+    if ((rc = ensure(P->sitems, (size_t)n_si * sizeof(int4), "item allocation"))) return rc;
+    if ((rc = ensure(P->sparts, (size_t)n_si * sizeof(int2), "item allocation"))) return rc;
+    if ((rc = ensure(P->rtiles, (size_t)n_rt * sizeof(int4), "item allocation"))) return rc;
+    ip.goff = go;
+    ip.soff = so;
+    ip.slotoff = slo;
+    ip.roff = ro;
+    ip.gitems = gi_tmp;
+    ip.gsize = gsize;
+    ip.gorder = gorder;
+    ip.sitems = si_tmp;
+    ip.sslot = sl_tmp;
+    ip.ssize = ssize;
+    ip.sorder = sorder;
+    ip.rtiles = reinterpret_cast<int4*>(P->rtiles.p);
+    GBN_CUDA(launch_bin_items(ip, s), "bin items launch");
+    // heaviest first, ties in bin order (a stable sort by chunk - count), as
+    // the host planner's stable_sort
+    GBN_CUDA(radix_sort_pairs(gsize, gorder, n_gi, bits_for(GATHER_CHUNK + 1), rtmp, s), "gather item sort");
+    GBN_CUDA(radix_sort_pairs(ssize, sorder, n_si, bits_for(SCH + 1), rtmp, s), "spread item sort");
+    GBN_CUDA(launch_permute_int4(gi_tmp, gorder, n_gi, reinterpret_cast<int4*>(P->gitems.p), s), "item order");
+    GBN_CUDA(launch_permute_int4(si_tmp, sorder, n_si, reinterpret_cast<int4*>(P->sitems.p), s), "item order");
+    GBN_CUDA(launch_permute_int2(sl_tmp, sorder, n_si, reinterpret_cast<int2*>(P->sparts.p), s), "item order");
+
+    // ---- lists (SoA, the layout of build_lists) --------------------------
+    P->has_phase = ph != nullptr;
+    if ((rc = ensure(P->glist, list_bytes<R>(P, M, false), "list allocation"))) return rc;
+    if ((rc = ensure(P->slist, list_bytes<R>(P, slen, true), "list allocation"))) return rc;
+    for (int which = 0; which < 2; ++which) {
+        const bool spread = which == 1;
+        const int64_t len = spread ? slen : M;
+        const ListLayout<R> L(P, len, spread);
+        char* base = reinterpret_cast<char*>(spread ? P->slist.p : P->glist.p);
+        PackParams<R> pk;
+        std::memset(&pk, 0, sizeof(pk));
+        pk.ndim = ndim;
+        pk.F = P->F;
+        pk.len = len;
+        pk.order = spread ? sval : gval;
+        pk.em = spread ? em : nullptr;
+        pk.els = spread ? els : nullptr;
+        pk.tm = tm;
+        pk.ph = ph;
+        pk.foff = reinterpret_cast<const int64_t*>(P->dfoff.p);
+        pk.ls_out = spread ? reinterpret_cast<short4*>(base + L.ls) : nullptr;
+        pk.ph_out = ph ? reinterpret_cast<C*>(base + L.ph) : nullptr;
+        for (int d = 0; d < ndim; ++d) pk.t_out[d] = reinterpret_cast<R*>(base + L.t[d]);
+        pk.idx_out = reinterpret_cast<int*>(base + L.idx);
+        GBN_CUDA(launch_bin_pack<R>(pk, s), "list pack launch");
+    }
+    P->glen = M;
+    P->slen = slen;
+    P->n_gitems = n_gi;
+    P->n_sitems = n_si;
+    P->n_rtiles = n_rt;
+    P->n_slots = n_slots;
+    return fill_coefs<R>(P, s, false);
 }
 
 }  // namespace
@@ -1350,6 +1604,29 @@ int gbn_plan_set_points(gbn_plan* P, const void* tm, const void* sample_phase) {
     // weights belong to the old coordinates
     GBN_CUDA(P->weights.alloc(0), "weight release");
     return P->dbl ? plan_points<double>(P, tm, sample_phase) : plan_points<float>(P, tm, sample_phase);
+}
+
+int gbn_plan_set_points_device(gbn_plan* P, const void* tm, const void* sample_phase, void* stream) {
+    if (!P) return fail(GBN_ERR_INVALID, "null plan");
+    if (!tm && P->M_total > 0) return fail(GBN_ERR_INVALID, "null coordinate array");
+    std::lock_guard<std::mutex> lk(P->mu);
+    DeviceGuard guard(P->device);
+    for (const void* q : {tm, sample_phase}) {
+        if (!q) continue;
+        cudaPointerAttributes a;
+        if (cudaPointerGetAttributes(&a, q) != cudaSuccess || a.type != cudaMemoryTypeDevice) {
+            cudaGetLastError();
+            return fail(GBN_ERR_INVALID, "gbn_plan_set_points_device takes device pointers");
+        }
+    }
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    // calls queued before on other streams may still read the lists
+    GBN_CUDA(cudaDeviceSynchronize(), "synchronise before replanning");
+    GBN_CUDA(P->weights.alloc(0), "weight release");
+    return P->dbl ? device_build_lists<double>(P, reinterpret_cast<const double*>(tm),
+                                               reinterpret_cast<const double2*>(sample_phase), s)
+                  : device_build_lists<float>(P, reinterpret_cast<const float*>(tm),
+                                              reinterpret_cast<const float2*>(sample_phase), s);
 }
 
 int gbn_plan_destroy(gbn_plan* P) {
