@@ -42,7 +42,7 @@ struct SpreadLayout {
 // One staged entry's contribution to a warp's register block: its value
 // for this lane's coil and the block's slice of its coefficient rows
 // (loaded), then B0 x B1 x B2 multiply-adds (accumulate).
-template <typename R, int NDIM, bool CX, typename SL>
+template <typename R, int NDIM, bool CX, typename SL, bool ROWSKIP = false>
 struct EntryOps {
     typedef typename Cx<R>::T C;
     static constexpr int B0 = SL::B0, B1 = SL::B1, B2 = SL::B2;
@@ -73,12 +73,16 @@ struct EntryOps {
         }
     }
 
+    // ROWSKIP: window start along axis 1 relative to the block, and the
+    // kernel width; rows of the block the window misses are skipped
+    int ry = 0, Jy = 0;
     template <int NB>
     __device__ __forceinline__ void accumulate(C (&acc)[NB]) const {
 #pragma unroll
         for (int k2 = 0; k2 < B2; ++k2) {
 #pragma unroll
             for (int k1 = 0; k1 < B1; ++k1) {
+                if (ROWSKIP && (unsigned)(k1 - ry) >= (unsigned)Jy) continue;
                 C tv;
                 if (CX) {
                     // conj(c2 c1) v, the pairs already hold conj
@@ -115,7 +119,7 @@ int spread_threads(int ndim, const int* T) {
     return 32 * warps;
 }
 
-template <typename R, int NDIM, bool CX, int JJ, int LSC>
+template <typename R, int NDIM, bool CX, int JJ, int LSC, bool ROWSKIP = false>
 __global__ void __launch_bounds__(256, 4)
 spread_kernel(const SpreadParams<R> p) {
     typedef typename Cx<R>::T C;
@@ -315,8 +319,12 @@ spread_kernel(const SpreadParams<R> p) {
                     if (kk == slot) pos = pk;
                 }
                 if (pos >= 0 && coil < nc) {
-                    EntryOps<R, NDIM, CX, SL> A;
+                    EntryOps<R, NDIM, CX, SL, ROWSKIP> A;
                     A.load(cp, vb, sls, gb + pos, VS, coil, bo0, bo1, bo2);
+                    if (ROWSKIP) {
+                        A.ry = sls[gb + pos].y - bo1;
+                        A.Jy = Jy;
+                    }
                     A.accumulate(acc);
                 }
             }
@@ -471,15 +479,15 @@ static cudaError_t ensure_smem(K kernel, size_t bytes) {
     return ensure_dynamic_smem(reinterpret_cast<const void*>(kernel), bytes);
 }
 
-template <typename R, int NDIM, bool CX, int JJ, int LSC>
+template <typename R, int NDIM, bool CX, int JJ, int LSC, bool ROWSKIP = false>
 static cudaError_t spread_launch(const SpreadParams<R>& p, cudaStream_t s) {
     const size_t smem = spread_smem(p.g, p.ln);
-    cudaError_t e = ensure_smem(spread_kernel<R, NDIM, CX, JJ, LSC>, smem);
+    cudaError_t e = ensure_smem(spread_kernel<R, NDIM, CX, JJ, LSC, ROWSKIP>, smem);
     if (e != cudaSuccess) return e;
     const int threads = spread_threads(NDIM, p.g.T);
     if (threads < 32 || threads > 256) return cudaErrorInvalidConfiguration;
     dim3 grid(p.nitems, (p.coils + p.ln.LS - 1) / p.ln.LS);
-    spread_kernel<R, NDIM, CX, JJ, LSC><<<grid, threads, smem, s>>>(p);
+    spread_kernel<R, NDIM, CX, JJ, LSC, ROWSKIP><<<grid, threads, smem, s>>>(p);
     return cudaGetLastError();
 }
 
@@ -504,6 +512,9 @@ static cudaError_t spread_specialised(const SpreadParams<float>& p, cudaStream_t
     for (int d = 1; d < p.g.ndim; ++d)
         if (p.g.J[d] != J) J = 0;
     const int LS = p.ln.LS;
+    // J 6, 32 coil lanes: skip the rows of a 4 x 4 block the window misses
+    // (measured at the 2-D 32-coil workload: 0.152 against 0.154 ms)
+    if (NDIM == 2 && J == 6 && LS == 32) return spread_launch<float, NDIM, false, 6, 32, true>(p, s);
 #define GBN_S(JV, LV) \
     if (J == JV && LS == LV) return spread_launch<float, NDIM, false, JV, LV>(p, s);
     GBN_S(6, 32) GBN_S(6, 16) GBN_S(6, 8) GBN_S(6, 1) GBN_S(4, 32) GBN_S(4, 16) GBN_S(4, 8) GBN_S(4, 1)

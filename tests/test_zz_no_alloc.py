@@ -130,7 +130,7 @@ def test_noalloc_leaves_device_memory_unchanged(gpu_lib):
 
 def test_noalloc_rejects_requests_beyond_its_capacity(gpu_lib):
     """2^18 samples on one k-space point: the four 16 x 8 spread tiles its
-    window touches are each split into 512 parts.  128 coils would need far
+    window touches are each split into 342 parts.  128 coils would need far
     more than the fixed 64 MiB and are refused before any launch (the output
     keeps its sentinel); 16 coils fit and match gbn_interp_adjoint."""
     from mrrt.nufft_gb300 import _lib
