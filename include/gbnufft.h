@@ -259,6 +259,17 @@ const char* gbn_last_error(void);
 /* Library version string. */
 const char* gbn_version(void);
 
+/* Testing hook, no counterpart in the reference: the bounds-check status of
+ * a plan in the checked build (libgbnufft_checked.so, compiled with
+ * GBN_CHECKED).  That build tests every global index its kernels form from
+ * plan data against the extent of the buffer it addresses, skips an access
+ * that fails, and records the failure as a bit in *out: 1 grid read, 2 grid
+ * write, 4 sample read, 8 sample write, 16 split-tile scratch, 32 list
+ * range, 64 image.  The call waits for the device, returns the bits
+ * recorded since the last call and clears them.  In the normal build it
+ * returns GBN_ERR_UNSUPPORTED with *out = 0.                               */
+int gbn_debug_check_status(gbn_plan* plan, unsigned* out);
+
 /* Testing hook, no counterpart in the reference: host-side fault injection
  * for the allocation-failure paths.  After this call, `after` more device
  * allocations made by the library succeed and the next one fails as if

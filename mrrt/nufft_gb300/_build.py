@@ -3,6 +3,11 @@
 The library is a plain C-ABI shared object (``include/gbnufft.h``); it links
 the CUDA runtime and cuFFT and nothing from PyTorch.  Translation units are
 compiled in parallel and linked once.
+
+``build(checked=True)`` compiles the same sources with ``GBN_CHECKED`` into
+``libgbnufft_checked.so``: every global index a kernel forms from plan data
+is tested against its buffer's extent, a failed test is recorded in the
+plan's status word (``gbn_debug_check_status``) and the access skipped.
 """
 import os
 import shutil
@@ -15,6 +20,8 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB_NAME = "libgbnufft.so"
 LIB_PATH = os.path.join(HERE, LIB_NAME)
+BUILD_CHECKED = os.path.join(HERE, "_build_checked")
+LIB_CHECKED_PATH = os.path.join(HERE, "libgbnufft_checked.so")
 
 SOURCES = ["gbn_plan.cu", "gbn_gather.cu", "gbn_spread.cu", "gbn_padcrop.cu", "gbn_dtft.cu", "gbn_grad.cu",
            "gbn_noalloc.cu", "gbn_coef.cu", "gbn_hostio.cu", "gbn_bin.cu", "gbn_sort.cu"]
@@ -48,18 +55,22 @@ def _stale(target, deps):
     return any(os.path.getmtime(d) > t for d in deps)
 
 
-def build(force=False, verbose=False):
-    """Compile every translation unit (in parallel) and link libgbnufft.so."""
-    os.makedirs(BUILD, exist_ok=True)
+def build(force=False, verbose=False, checked=False):
+    """Compile every translation unit (in parallel) and link libgbnufft.so
+    (or, with ``checked``, libgbnufft_checked.so)."""
+    build_dir = BUILD_CHECKED if checked else BUILD
+    lib_path = LIB_CHECKED_PATH if checked else LIB_PATH
+    defines = ["-DGBN_CHECKED"] if checked else []
+    os.makedirs(build_dir, exist_ok=True)
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
     headers.append(os.path.join(os.path.dirname(os.path.dirname(HERE)), "include", "gbnufft.h"))
     objs, jobs = [], []
     for src in SOURCES:
         s = os.path.join(CSRC, src)
-        o = os.path.join(BUILD, src.replace(".cu", ".o"))
+        o = os.path.join(build_dir, src.replace(".cu", ".o"))
         objs.append(o)
         if force or _stale(o, [s] + headers):
-            jobs.append([nvcc()] + ARCH + FLAGS + ["-c", s, "-o", o])
+            jobs.append([nvcc()] + ARCH + FLAGS + defines + ["-c", s, "-o", o])
 
     def run(cmd):
         r = subprocess.run(cmd, capture_output=True, text=True)
@@ -71,14 +82,22 @@ def build(force=False, verbose=False):
     if jobs:
         with ThreadPoolExecutor(max_workers=min(len(jobs), os.cpu_count() or 4)) as ex:
             list(ex.map(run, jobs))
-    if force or jobs or _stale(LIB_PATH, objs):
-        tmp = LIB_PATH + ".tmp"
+    if force or jobs or _stale(lib_path, objs):
+        tmp = lib_path + ".tmp"
         cmd = [nvcc()] + ARCH + ["-shared", "-o", tmp] + objs + [
             "-L" + _cuda_lib_dir(), "-lcufft", "-lcudart"]
         run(cmd)
-        os.replace(tmp, LIB_PATH)
-    return LIB_PATH
+        os.replace(tmp, lib_path)
+    return lib_path
+
+
+def build_all(force=False, verbose=False):
+    """Both libraries, the normal and the checked build, compiled together."""
+    with ThreadPoolExecutor(max_workers=2) as ex:
+        a = ex.submit(build, force, verbose, False)
+        b = ex.submit(build, force, verbose, True)
+        return a.result(), b.result()
 
 
 if __name__ == "__main__":
-    print(build(force="--force" in sys.argv, verbose=True))
+    print(build(force="--force" in sys.argv, verbose=True, checked="--checked" in sys.argv))

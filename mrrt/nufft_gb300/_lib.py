@@ -88,36 +88,55 @@ SIGNATURES = {
     "gbn_last_error": [],
     "gbn_version": [],
     "gbn_debug_fail_alloc": [ctypes.c_longlong],
+    "gbn_debug_check_status": [_VP, ctypes.POINTER(ctypes.c_uint)],
 }
 
 _lib = None
+_lib_checked = None
 _lock = threading.Lock()
+
+
+def _open(path):
+    if not os.path.exists(path):
+        raise ImportError(
+            "%s is not built; run mrrt.nufft_gb300._build.build() "
+            "or __graft_entry__.build() first" % path)
+    lib = ctypes.CDLL(path)
+    for name, args in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = ctypes.c_char_p if name in ("gbn_last_error", "gbn_version") else ctypes.c_int
+    return lib
 
 
 def load(path=None):
     """Load (once) and return the ctypes handle of libgbnufft.so."""
     global _lib
     with _lock:
-        if _lib is not None:
-            return _lib
-        path = path or LIB_PATH
-        if not os.path.exists(path):
-            raise ImportError(
-                "libgbnufft.so is not built (%s); run mrrt.nufft_gb300._build.build() "
-                "or __graft_entry__.build() first" % path)
-        lib = ctypes.CDLL(path)
-        for name, args in SIGNATURES.items():
-            fn = getattr(lib, name)
-            fn.argtypes = args
-            fn.restype = ctypes.c_char_p if name in ("gbn_last_error", "gbn_version") else ctypes.c_int
-        _lib = lib
-        return lib
+        if _lib is None:
+            _lib = _open(path or LIB_PATH)
+        return _lib
 
 
-def check(rc):
+def load_checked():
+    """Load (once) the bounds-checked build, libgbnufft_checked.so (a
+    separate library: plans made through it run the checked kernels)."""
+    global _lib_checked
+    with _lock:
+        if _lib_checked is None:
+            _lib_checked = _open(os.path.join(os.path.dirname(LIB_PATH), "libgbnufft_checked.so"))
+        return _lib_checked
+
+
+def check(rc, lib=None):
     if rc != GBN_OK:
-        msg = load().gbn_last_error().decode(errors="replace")
+        msg = (lib or load()).gbn_last_error().decode(errors="replace")
         if rc in (GBN_ERR_INVALID, GBN_ERR_UNSUPPORTED, GBN_ERR_TOOLARGE):
             raise GbnValueError(rc, msg)
         raise GbnError(rc, msg)
     return rc
+
+
+def check_with(lib, rc):
+    """check() with the error message taken from ``lib``."""
+    return check(rc, lib)

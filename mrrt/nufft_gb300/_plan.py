@@ -39,9 +39,12 @@ class GpuPlan:
 
     def __init__(self, Nd, Kd, Jd, L, rdt, tables_re, tables_im, sn, tm, sample_phase,
                  frame_offsets=None, ortho=False, adjoint_scale=1.0, pb_coef=None, pb_order=None,
-                 phasing="real", max_coils=1, tile=None, stile=None, device=None, table_only=False):
+                 phasing="real", max_coils=1, tile=None, stile=None, device=None, table_only=False,
+                 lib=None):
         require_cuda()
-        self.lib = _lib.load()
+        # lib: a loaded libgbnufft (default); _lib.load_checked() gives the
+        # bounds-checked build
+        self.lib = lib if lib is not None else _lib.load()
         self.rdt = np.dtype(rdt)
         self.ndim = len(Nd)
         self.Nd, self.Kd, self.Jd = tuple(Nd), tuple(Kd), tuple(Jd)
@@ -81,7 +84,7 @@ class GpuPlan:
             ph = np.ascontiguousarray(sample_phase, dtype=np.result_type(self.rdt, np.complex64))
         handle = ctypes.c_void_p()
         with torch.cuda.device(self.device):
-            _lib.check(self.lib.gbn_plan_create(
+            _lib.check_with(self.lib, self.lib.gbn_plan_create(
                 ctypes.byref(handle), ctypes.byref(g), Hre, Him, _vp(sn),
                 fo.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), _vp(tm), _vp(ph),
                 self.device.index))
@@ -115,7 +118,7 @@ class GpuPlan:
         self._check(x, F * coils * self.Nprod, "x")
         self._check(y, coils * self.M_total, "y")
         with torch.cuda.device(self.device):
-            _lib.check(self.lib.gbn_forward(self.handle, ctypes.c_void_p(x.data_ptr()),
+            _lib.check_with(self.lib, self.lib.gbn_forward(self.handle, ctypes.c_void_p(x.data_ptr()),
                                             ctypes.c_void_p(y.data_ptr()), int(coils), _stream()))
         return y
 
@@ -124,7 +127,7 @@ class GpuPlan:
         self._check(y, coils * self.M_total, "y")
         self._check(x, F * coils * self.Nprod, "x")
         with torch.cuda.device(self.device):
-            _lib.check(self.lib.gbn_adjoint(self.handle, ctypes.c_void_p(y.data_ptr()),
+            _lib.check_with(self.lib, self.lib.gbn_adjoint(self.handle, ctypes.c_void_p(y.data_ptr()),
                                             ctypes.c_void_p(x.data_ptr()), int(coils), _stream()))
         return x
 
@@ -146,7 +149,7 @@ class GpuPlan:
         self._check_host(x, F * coils * self.Nprod, "x")
         self._check_host(y, coils * self.M_total, "y")
         with torch.cuda.device(self.device):
-            _lib.check(self.lib.gbn_forward_host(self.handle, ctypes.c_void_p(x.data_ptr()),
+            _lib.check_with(self.lib, self.lib.gbn_forward_host(self.handle, ctypes.c_void_p(x.data_ptr()),
                                                  ctypes.c_void_p(y.data_ptr()), int(coils), _stream()))
         return y
 
@@ -156,7 +159,7 @@ class GpuPlan:
         self._check_host(y, coils * self.M_total, "y")
         self._check_host(x, F * coils * self.Nprod, "x")
         with torch.cuda.device(self.device):
-            _lib.check(self.lib.gbn_adjoint_host(self.handle, ctypes.c_void_p(y.data_ptr()),
+            _lib.check_with(self.lib, self.lib.gbn_adjoint_host(self.handle, ctypes.c_void_p(y.data_ptr()),
                                                  ctypes.c_void_p(x.data_ptr()), int(coils), _stream()))
         return x
 
@@ -168,7 +171,7 @@ class GpuPlan:
         self._check(maps, coils * self.Nprod, "maps")
         self._check(y, coils * self.M_total, "y")
         with torch.cuda.device(self.device):
-            _lib.check(self.lib.gbn_forward_sense(self.handle, ctypes.c_void_p(image.data_ptr()),
+            _lib.check_with(self.lib, self.lib.gbn_forward_sense(self.handle, ctypes.c_void_p(image.data_ptr()),
                                                   ctypes.c_void_p(maps.data_ptr()),
                                                   ctypes.c_void_p(y.data_ptr()), int(coils), _stream()))
         return y
@@ -181,7 +184,7 @@ class GpuPlan:
         self._check(maps, coils * self.Nprod, "maps")
         self._check(image, F * self.Nprod, "image")
         with torch.cuda.device(self.device):
-            _lib.check(self.lib.gbn_adjoint_sense(self.handle, ctypes.c_void_p(y.data_ptr()),
+            _lib.check_with(self.lib, self.lib.gbn_adjoint_sense(self.handle, ctypes.c_void_p(y.data_ptr()),
                                                   ctypes.c_void_p(maps.data_ptr()),
                                                   ctypes.c_void_p(image.data_ptr()), int(coils), _stream()))
         return image
@@ -191,7 +194,7 @@ class GpuPlan:
         self._check(grid, F * coils * self.Kprod, "grid")
         self._check(y, coils * self.M_total, "y")
         with torch.cuda.device(self.device):
-            _lib.check(self.lib.gbn_interp_forward(self.handle, ctypes.c_void_p(grid.data_ptr()),
+            _lib.check_with(self.lib, self.lib.gbn_interp_forward(self.handle, ctypes.c_void_p(grid.data_ptr()),
                                                    ctypes.c_void_p(y.data_ptr()), int(coils),
                                                    _stream()))
         return y
@@ -201,7 +204,7 @@ class GpuPlan:
         self._check(y, coils * self.M_total, "y")
         self._check(grid, F * coils * self.Kprod, "grid")
         with torch.cuda.device(self.device):
-            _lib.check(self.lib.gbn_interp_adjoint(self.handle, ctypes.c_void_p(y.data_ptr()),
+            _lib.check_with(self.lib, self.lib.gbn_interp_adjoint(self.handle, ctypes.c_void_p(y.data_ptr()),
                                                    ctypes.c_void_p(grid.data_ptr()), int(coils),
                                                    _stream()))
         return grid
@@ -209,7 +212,7 @@ class GpuPlan:
     def forward_grid(self, coils):
         """View of the plan's grid buffer after a forward call: [coils, Kprod]."""
         ptr = ctypes.c_void_p()
-        _lib.check(self.lib.gbn_forward_grid(self.handle, ctypes.byref(ptr)))
+        _lib.check_with(self.lib, self.lib.gbn_forward_grid(self.handle, ctypes.byref(ptr)))
         return ptr.value
 
     def set_dtables(self, dtabs):
@@ -217,13 +220,13 @@ class GpuPlan:
         self._keep += arrs
         D = (ctypes.c_void_p * 3)(*[_vp(a) for a in arrs] + [None] * (3 - len(arrs)))
         with torch.cuda.device(self.device):
-            _lib.check(self.lib.gbn_plan_set_dtables(self.handle, D))
+            _lib.check_with(self.lib, self.lib.gbn_plan_set_dtables(self.handle, D))
 
     def grad_tm(self, grid_ptr, gy, phase_shift, gtm, coils):
         self._check(gy, coils * self.M_total, "gy")
         sh = (ctypes.c_double * 3)(*[float(s) for s in phase_shift] + [0.0] * (3 - len(phase_shift)))
         with torch.cuda.device(self.device):
-            _lib.check(self.lib.gbn_grad_tm(self.handle, ctypes.c_void_p(grid_ptr),
+            _lib.check_with(self.lib, self.lib.gbn_grad_tm(self.handle, ctypes.c_void_p(grid_ptr),
                                             ctypes.c_void_p(gy.data_ptr()), sh,
                                             ctypes.c_void_p(gtm.data_ptr()), int(coils), _stream()))
         return gtm
@@ -233,14 +236,14 @@ class GpuPlan:
         replace the table interpolation; ``None`` returns to table mode."""
         if w_re is None:
             with torch.cuda.device(self.device):
-                _lib.check(self.lib.gbn_plan_set_weights(self.handle, None, None))
+                _lib.check_with(self.lib, self.lib.gbn_plan_set_weights(self.handle, None, None))
             return
         wr = [np.ascontiguousarray(w, dtype=self.rdt) for w in w_re]
         wi = [np.ascontiguousarray(w, dtype=self.rdt) for w in w_im] if w_im is not None else None
         Wr = (ctypes.c_void_p * 3)(*[_vp(w) for w in wr] + [None] * (3 - len(wr)))
         Wi = (ctypes.c_void_p * 3)(*[_vp(w) for w in wi] + [None] * (3 - len(wi))) if wi else None
         with torch.cuda.device(self.device):
-            _lib.check(self.lib.gbn_plan_set_weights(self.handle, Wr, Wi))
+            _lib.check_with(self.lib, self.lib.gbn_plan_set_weights(self.handle, Wr, Wi))
 
     def set_points(self, tm, sample_phase):
         tm = np.ascontiguousarray(tm, dtype=self.rdt).reshape(-1, self.ndim)
@@ -251,7 +254,7 @@ class GpuPlan:
         if sample_phase is not None:
             ph = np.ascontiguousarray(sample_phase, dtype=np.result_type(self.rdt, np.complex64))
         with torch.cuda.device(self.device):
-            _lib.check(self.lib.gbn_plan_set_points(self.handle, _vp(tm), _vp(ph)))
+            _lib.check_with(self.lib, self.lib.gbn_plan_set_points(self.handle, _vp(tm), _vp(ph)))
 
     def set_points_device(self, tm, sample_phase=None):
         """Replace the coordinates from device tensors (``tm`` [M_total, ndim]
@@ -269,13 +272,13 @@ class GpuPlan:
             if ph.numel() != self.M_total:
                 raise ValueError("sample_phase needs %d values" % self.M_total)
         with torch.cuda.device(self.device):
-            _lib.check(self.lib.gbn_plan_set_points_device(
+            _lib.check_with(self.lib, self.lib.gbn_plan_set_points_device(
                 self.handle, ctypes.c_void_p(tm.data_ptr()),
                 ctypes.c_void_p(ph.data_ptr()) if ph is not None else None, _stream()))
 
     def stats(self):
         out = (ctypes.c_int64 * 8)()
-        _lib.check(self.lib.gbn_plan_stats(self.handle, out))
+        _lib.check_with(self.lib, self.lib.gbn_plan_stats(self.handle, out))
         keys = ("gather_items", "spread_items", "split_tiles", "gather_len", "spread_len",
                 "tiles", "device_bytes", "samples")
         return dict(zip(keys, list(out)))

@@ -6,6 +6,17 @@
 
 #include "gbn_internal.h"
 
+// Checked builds (compiled with GBN_CHECKED, libgbnufft_checked.so): every
+// global index the kernels form from plan data is tested against the extent
+// of its buffer before the access.  A failed test sets a bit in the plan's
+// status word (gbn_debug_check_status) and the access is skipped: nothing
+// traps or faults.  In the normal build the test is the constant true.
+#ifdef GBN_CHECKED
+#define GBN_INB(word, cond, bit) ((cond) ? true : (atomicOr((word), (bit)), false))
+#else
+#define GBN_INB(word, cond, bit) true
+#endif
+
 namespace gbn {
 
 __device__ __forceinline__ float2 cmul(float2 a, float2 b) {

@@ -72,6 +72,7 @@ gather_kernel(const GatherParams<R> p) {
 
     const int4 it = p.items[blockIdx.x];
     const int f = it.x, tile = it.y, start = it.z, count = it.w;
+    if (!GBN_INB(g.check, start >= 0 && count >= 0 && start + (int64_t)count <= p.s.len, CHK_LIST)) return;
     const int LS = LSC > 0 ? LSC : p.ln.LS;
     const int lsh = LSC > 0 ? (LSC == 32 ? 5 : LSC == 16 ? 4 : LSC == 8 ? 3 : LSC == 4 ? 2 : LSC == 2 ? 1 : 0)
                             : p.ln.lsh;
@@ -129,7 +130,11 @@ gather_kernel(const GatherParams<R> p) {
             for (int u = 0; u < 8; ++u) {
                 cc[u] = c;
                 cl[u] = cell;
-                if (e + u * step < E) v[u] = gb[(int64_t)c * g.gsp + soff[cell]];
+                if (e + u * step < E) {
+                    const int64_t gi = ((int64_t)f * p.coils + c0 + c) * g.gsp + soff[cell];
+                    if (GBN_INB(g.check, gi >= 0 && gi < g.grid_elems, CHK_GRID_READ))
+                        v[u] = gb[(int64_t)c * g.gsp + soff[cell]];
+                }
                 cell += step;
                 while (cell >= Rtot) cell -= Rtot, ++c;
             }
@@ -167,7 +172,11 @@ gather_kernel(const GatherParams<R> p) {
             C v[4];
 #pragma unroll
             for (int u = 0; u < 4; ++u)
-                if (c + u < nc) v[u] = src[(int64_t)(c + u) * g.gsp];
+                if (c + u < nc) {
+                    const int64_t gi = ((int64_t)f * p.coils + c0 + c + u) * g.gsp + off;
+                    if (GBN_INB(g.check, gi >= 0 && gi < g.grid_elems, CHK_GRID_READ))
+                        v[u] = src[(int64_t)(c + u) * g.gsp];
+                }
 #pragma unroll
             for (int u = 0; u < 4; ++u) {
                 if (c + u < nc) {
@@ -193,6 +202,7 @@ gather_kernel(const GatherParams<R> p) {
     const int th = TS ? (lane >> 3) & 1 : 0;   // tap half (tap split)
     const int64_t fo = p.foff[f];
     const int Mf = (int)(p.foff[f + 1] - fo);
+    if (!GBN_INB(g.check, (fo + Mf) * p.coils <= g.sample_elems, CHK_SAMPLE_WRITE)) return;
     C* yb = p.y + fo * p.coils + (int64_t)(c0 + coil) * Mf;
     const int J0 = JJ > 0 ? JJ : g.J[0];
     const int J1 = JJ > 0 ? JJ : g.J[NDIM > 1 ? 1 : 0];
@@ -349,19 +359,19 @@ gather_kernel(const GatherParams<R> p) {
                     // (enabled where measured faster: 32 lanes, and 3-D)
                     if (pidx >= 0 && idx == pidx + 1 &&
                         (reinterpret_cast<uintptr_t>(yb + pidx) & 15) == 0) {
-                        store_pair(yb + pidx, pacc, acc);
+                        if (GBN_INB(g.check, idx < Mf, CHK_SAMPLE_WRITE)) store_pair(yb + pidx, pacc, acc);
                         pidx = -1;
                     } else {
                         if (pidx >= 0) yb[pidx] = pacc;
                         pidx = -1;
-                        if ((idx & 1) == 0) {
+                        if ((idx & 1) == 0 && GBN_INB(g.check, idx >= 0 && idx < Mf, CHK_SAMPLE_WRITE)) {
                             pidx = idx;
                             pacc = acc;
-                        } else {
+                        } else if (GBN_INB(g.check, idx >= 0 && idx < Mf, CHK_SAMPLE_WRITE)) {
                             yb[idx] = acc;
                         }
                     }
-                } else {
+                } else if (GBN_INB(g.check, idx >= 0 && idx < Mf, CHK_SAMPLE_WRITE)) {
                     yb[idx] = acc;
                 }
             }

@@ -43,7 +43,15 @@ struct Geom {
     int64_t gsp, gs1, gs2;
     R pbc[3];                // phase_before coefficient per memory axis
     int pbo[3];              // summation order of the per-axis phases
+    // Checked builds (GBN_CHECKED): the plan's status word and the extents
+    // (complex elements) of the grid and sample buffers of the call
+    unsigned* check;
+    int64_t grid_elems, sample_elems;
 };
+
+// Status bits of a checked build: which kind of index failed its bound.
+constexpr unsigned CHK_GRID_READ = 1u, CHK_GRID_WRITE = 2u, CHK_SAMPLE_READ = 4u, CHK_SAMPLE_WRITE = 8u,
+                   CHK_SCRATCH = 16u, CHK_LIST = 32u, CHK_IMAGE = 64u;
 
 // Coil-lane layout of a CTA: LS lanes per sample (power of two <= 32),
 // SW = 32 / LS samples per warp.  Staged grid values for one cell occupy
@@ -66,6 +74,7 @@ struct SampleList {
     const R* cr;
     const R* ci;
     int jsum;
+    int64_t len;                    // entries in the list
 };
 
 // Fill a list's precomputed coefficients, for every entry of every work
@@ -117,6 +126,7 @@ struct SpreadParams {
     typename Cx<R>::T* grid;
     typename Cx<R>::T* scratch;     // [slot][chunk][LS][tile cells] partial sums
     int64_t tile_cells;             // T0*T1*T2
+    int64_t scratch_elems;          // scratch extent (complex elements)
     int apply_pb;
     int apply_ph;
 };
@@ -131,6 +141,7 @@ struct ReduceParams {
     const typename Cx<R>::T* scratch;
     typename Cx<R>::T* grid;
     int64_t tile_cells;
+    int64_t scratch_elems;
     int apply_pb;
 };
 
@@ -148,6 +159,8 @@ struct PadParams {
     // f * coils + c receives sn * maps[c] * x[f]; nullptr for the plain pad
     const typename Cx<R>::T* maps;
     int coils;
+    unsigned* check;                // checked builds: status word
+    int64_t x_elems, out_elems;     // extents of x and out
 };
 
 template <typename R>
@@ -165,6 +178,8 @@ struct CropParams {
     // + c), one image per frame; nullptr for the plain crop
     const typename Cx<R>::T* maps;
     int coils;
+    unsigned* check;                // checked builds: status word
+    int64_t grid_elems, x_elems;    // extents of grid and x
 };
 
 template <typename R>

@@ -37,9 +37,14 @@ __global__ void __launch_bounds__(256) pad_kernel(const PadParams<R> p) {
         const int64_t rr = row - pl * rows_per_plane;
         const int n1 = (int)(rr % p.N[1]);
         const int n2 = (int)(rr / p.N[1]);
-        const C* src = p.x + pl * p.Nprod + rr * p.N[0];
+        const int64_t xo = pl * p.Nprod + rr * p.N[0];
+        const int64_t oo = pl * p.gsp + (int64_t)n1 * p.gs1 + (int64_t)n2 * p.gs2;
+        if (!GBN_INB(p.check, xo + p.N[0] <= p.x_elems, CHK_IMAGE) ||
+            !GBN_INB(p.check, oo + p.N[0] <= p.out_elems, CHK_GRID_WRITE))
+            continue;
+        const C* src = p.x + xo;
         const R* s = p.sn + rr * p.N[0];
-        C* dst = p.out + pl * p.gsp + (int64_t)n1 * p.gs1 + (int64_t)n2 * p.gs2;
+        C* dst = p.out + oo;
         if constexpr (PAIRS) {
             const float4* s4 = reinterpret_cast<const float4*>(src);
             const float2* w2 = reinterpret_cast<const float2*>(s);
@@ -80,9 +85,14 @@ __global__ void __launch_bounds__(256) crop_kernel(const CropParams<R> p) {
         const int64_t rr = row - pl * rows_per_plane;
         const int n1 = (int)(rr % p.N[1]);
         const int n2 = (int)(rr / p.N[1]);
-        const C* src = p.grid + pl * p.gsp + (int64_t)n1 * p.gs1 + (int64_t)n2 * p.gs2;
+        const int64_t go = pl * p.gsp + (int64_t)n1 * p.gs1 + (int64_t)n2 * p.gs2;
+        const int64_t xo = pl * p.Nprod + rr * p.N[0];
+        if (!GBN_INB(p.check, go + p.N[0] <= p.grid_elems, CHK_GRID_READ) ||
+            !GBN_INB(p.check, xo + p.N[0] <= p.x_elems, CHK_IMAGE))
+            continue;
+        const C* src = p.grid + go;
         const R* s = p.sn + rr * p.N[0];
-        C* dst = p.x + pl * p.Nprod + rr * p.N[0];
+        C* dst = p.x + xo;
         if constexpr (PAIRS) {
             const float4* s4 = reinterpret_cast<const float4*>(src);
             const float2* w2 = reinterpret_cast<const float2*>(s);
@@ -141,10 +151,14 @@ __global__ void __launch_bounds__(256) pad_sense_kernel(const PadParams<R> p) {
         const int64_t f = pl / p.coils, c = pl - f * p.coils;
         const int n1 = (int)(rr % p.N[1]);
         const int n2 = (int)(rr / p.N[1]);
+        const int64_t oo = pl * p.gsp + (int64_t)n1 * p.gs1 + (int64_t)n2 * p.gs2;
+        if (!GBN_INB(p.check, (f * p.Nprod + rr * p.N[0]) + p.N[0] <= p.x_elems, CHK_IMAGE) ||
+            !GBN_INB(p.check, oo + p.N[0] <= p.out_elems, CHK_GRID_WRITE))
+            continue;
         const C* src = p.x + f * p.Nprod + rr * p.N[0];
         const C* mp = p.maps + c * p.Nprod + rr * p.N[0];
         const R* s = p.sn + rr * p.N[0];
-        C* dst = p.out + pl * p.gsp + (int64_t)n1 * p.gs1 + (int64_t)n2 * p.gs2;
+        C* dst = p.out + oo;
         for (int n0 = lane; n0 < p.N[0]; n0 += 32) {
             C v = cmul(src[n0], mp[n0]);
             const R w = s[n0];
@@ -172,6 +186,9 @@ __global__ void __launch_bounds__(256) crop_sense_kernel(const CropParams<R> p) 
         const int n1 = (int)(rr % p.N[1]);
         const int n2 = (int)(rr / p.N[1]);
         const int64_t goff = (int64_t)n1 * p.gs1 + (int64_t)n2 * p.gs2;
+        if (!GBN_INB(p.check, ((f + 1) * p.coils - 1) * p.gsp + goff + p.N[0] <= p.grid_elems, CHK_GRID_READ) ||
+            !GBN_INB(p.check, f * p.Nprod + rr * p.N[0] + p.N[0] <= p.x_elems, CHK_IMAGE))
+            continue;
         const R* s = p.sn + rr * p.N[0];
         C* dst = p.x + f * p.Nprod + rr * p.N[0];
         for (int n0 = lane; n0 < p.N[0]; n0 += 32) {

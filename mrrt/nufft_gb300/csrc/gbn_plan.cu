@@ -184,6 +184,7 @@ struct gbn_plan {
     bool has_phase = false;
 
     DevBuf tables, dtables, sn, dfoff;
+    DevBuf check;         // status word of the checked build's bounds tests
     DevBuf weights;       // sparse-matrix mode: per-axis [M_total][J] weights (re, then im)
     DevBuf gcoef, scoef;  // precomputed coefficients in gather / spread list order
     bool coefs = false;   // gcoef / scoef hold the current lists' coefficients
@@ -272,6 +273,7 @@ Geom<R> make_geom(const gbn_plan* P, bool spread) {
     g.gsp = P->Kprod;
     g.gs1 = g.K[0];
     g.gs2 = (int64_t)g.K[0] * g.K[1];
+    g.check = reinterpret_cast<unsigned*>(P->check.p);
     return g;
 }
 
@@ -345,6 +347,7 @@ SampleList<R> make_list(const gbn_plan* P, const DevBuf& buf, int64_t len, bool 
     if (P->has_phase) s.ph = reinterpret_cast<const C*>(b + L.ph);
     for (int d = 0; d < P->geom.ndim; ++d) s.t[d] = reinterpret_cast<const R*>(b + L.t[d]);
     s.idx = reinterpret_cast<const int*>(b + L.idx);
+    s.len = len;
     if (P->coefs) {
         const DevBuf& cb = with_ls ? P->scoef : P->gcoef;
         int jsum = 0;
@@ -846,6 +849,8 @@ int run_gather(gbn_plan* P, const void* grid, void* y, int coils, bool phases, c
     p.apply_pb = phases && P->geom.phasing == GBN_PHASING_REAL;
     p.grid_scale = (phases && P->geom.ortho) ? (R)std::sqrt((double)P->Kprod) : (R)1;
     p.apply_ph = phases && P->has_phase;
+    p.g.grid_elems = (int64_t)P->F * coils * P->Kprod;
+    p.g.sample_elems = (int64_t)coils * P->M_total;
     GBN_CUDA(launch_gather<R>(p, s), "gather launch");
     return GBN_OK;
 }
@@ -870,6 +875,9 @@ int run_spread(gbn_plan* P, const void* y, void* grid, int coils, bool phases, c
     p.grid = reinterpret_cast<C*>(grid);
     p.scratch = reinterpret_cast<C*>(P->scratch.p);
     p.tile_cells = (int64_t)P->Ts[0] * P->Ts[1] * P->Ts[2];
+    p.scratch_elems = P->scratch_cap;
+    p.g.grid_elems = (int64_t)P->F * coils * P->Kprod;
+    p.g.sample_elems = (int64_t)coils * P->M_total;
     p.apply_pb = phases && P->geom.phasing == GBN_PHASING_REAL;
     p.apply_ph = phases && P->has_phase;
     GBN_CUDA(launch_spread<R>(p, s), "spread launch");
@@ -884,6 +892,7 @@ int run_spread(gbn_plan* P, const void* y, void* grid, int coils, bool phases, c
         q.scratch = p.scratch;
         q.grid = p.grid;
         q.tile_cells = p.tile_cells;
+        q.scratch_elems = p.scratch_elems;
         q.apply_pb = p.apply_pb;
         GBN_CUDA(launch_reduce<R>(q, s), "reduce launch");
     }
@@ -927,6 +936,9 @@ int run_spread_noalloc(gbn_plan* P, const void* y, void* grid, int coils, cudaSt
     p.grid = reinterpret_cast<C*>(grid);
     p.scratch = reinterpret_cast<C*>(scratch);
     p.tile_cells = tile_cells;
+    p.scratch_elems = (int64_t)(cap / sizeof(C));
+    p.g.grid_elems = (int64_t)P->F * coils * P->Kprod;
+    p.g.sample_elems = (int64_t)coils * P->M_total;
     p.apply_pb = 0;
     p.apply_ph = 0;
     GBN_CUDA(launch_spread<R>(p, s), "no-alloc spread launch");
@@ -941,6 +953,7 @@ int run_spread_noalloc(gbn_plan* P, const void* y, void* grid, int coils, cudaSt
         q.scratch = p.scratch;
         q.grid = p.grid;
         q.tile_cells = p.tile_cells;
+        q.scratch_elems = p.scratch_elems;
         q.apply_pb = 0;
         GBN_CUDA(launch_reduce<R>(q, s), "no-alloc reduce launch");
     }
@@ -968,6 +981,9 @@ int run_forward(gbn_plan* P, const void* x, void* y, int coils, cudaStream_t s, 
     pp.out = reinterpret_cast<typename Cx<R>::T*>(P->pad.p);
     pp.maps = reinterpret_cast<const typename Cx<R>::T*>(maps);
     pp.coils = coils;
+    pp.check = reinterpret_cast<unsigned*>(P->check.p);
+    pp.x_elems = (int64_t)(maps ? P->F : P->F * coils) * P->Nprod;
+    pp.out_elems = (int64_t)P->cap_planes * P->Kprod;
     internal_layout(P, P->F * coils, pp);
     {
         NvtxRange r("gbn forward: pad");
@@ -1014,6 +1030,9 @@ int run_adjoint(gbn_plan* P, const void* y, void* x, int coils, cudaStream_t s, 
     cp.x = reinterpret_cast<typename Cx<R>::T*>(x);
     cp.maps = reinterpret_cast<const typename Cx<R>::T*>(maps);
     cp.coils = coils;
+    cp.check = reinterpret_cast<unsigned*>(P->check.p);
+    cp.x_elems = (int64_t)(maps ? P->F : P->F * coils) * P->Nprod;
+    cp.grid_elems = (int64_t)P->cap_planes * P->Kprod;
     internal_layout(P, P->F * coils, cp);
     NvtxRange r("gbn adjoint: crop");
     GBN_CUDA(launch_crop<R>(cp, s), "crop launch");
@@ -1591,6 +1610,14 @@ int gbn_plan_create(gbn_plan** out, const gbn_geometry* geom, const void* const*
         P->Nprod *= geom->Nd[d];
     }
     choose_tiles(P);
+    {
+        cudaError_t e = P->check.alloc(16);
+        if (e == cudaSuccess) e = cudaMemset(P->check.p, 0, 16);
+        if (e != cudaSuccess) {
+            delete P;
+            return cuda_fail(e, "status word");
+        }
+    }
     rc = P->dbl ? upload_static<double>(P, h_re, h_im, sn) : upload_static<float>(P, h_re, h_im, sn);
     if (!rc) rc = P->dbl ? plan_points<double>(P, tm, sample_phase) : plan_points<float>(P, tm, sample_phase);
     if (rc) {
@@ -1852,6 +1879,21 @@ int gbn_plan_stats(const gbn_plan* P, int64_t* o) {
                      P->grid.bytes + P->scratch.bytes);
     o[7] = P->M_total;
     return GBN_OK;
+}
+
+int gbn_debug_check_status(gbn_plan* P, unsigned* out) {
+    if (!P || !out) return fail(GBN_ERR_INVALID, "null argument");
+    *out = 0;
+#ifdef GBN_CHECKED
+    std::lock_guard<std::mutex> lk(P->mu);
+    DeviceGuard guard(P->device);
+    GBN_CUDA(cudaDeviceSynchronize(), "status read");
+    GBN_CUDA(cudaMemcpy(out, P->check.p, sizeof(unsigned), cudaMemcpyDeviceToHost), "status read");
+    GBN_CUDA(cudaMemset(P->check.p, 0, sizeof(unsigned)), "status reset");
+    return GBN_OK;
+#else
+    return fail(GBN_ERR_UNSUPPORTED, "bounds checks are compiled only into libgbnufft_checked.so");
+#endif
 }
 
 const char* gbn_last_error(void) { return g_last_error.c_str(); }

@@ -151,6 +151,7 @@ spread_kernel(const SpreadParams<R> p) {
     const int4 it = p.items[blockIdx.x];
     const int2 part = p.parts[blockIdx.x];
     const int f = it.x, tile = it.y, start = it.z, count = it.w;
+    if (!GBN_INB(g.check, start >= 0 && count >= 0 && start + (int64_t)count <= p.s.len, CHK_LIST)) return;
     const int c0 = blockIdx.y << lsh;
     const int nc = min(LS, p.coils - c0);
 
@@ -178,6 +179,7 @@ spread_kernel(const SpreadParams<R> p) {
 
     const int64_t fo = p.foff[f];
     const int Mf = (int)(p.foff[f + 1] - fo);
+    if (!GBN_INB(g.check, (fo + Mf) * p.coils <= g.sample_elems, CHK_SAMPLE_READ)) return;
     const C* yb = p.y + fo * p.coils + (int64_t)c0 * Mf;
 
     // zero padding of the coefficient rows: written once, the J coefficient
@@ -220,7 +222,7 @@ spread_kernel(const SpreadParams<R> p) {
 #pragma unroll
         for (int u = 0; u < 2; ++u) {
             const int el = elo + u * nthr;
-            if (u < EPT && el < n) {
+            if (u < EPT && el < n && GBN_INB(g.check, nidx[u] >= 0 && nidx[u] < Mf, CHK_SAMPLE_READ)) {
                 const C* src = yb + nidx[u];
                 for (int c = cg; c < nc; c += ng) cp_async<sizeof(C)>(vb + el * VS + c, src + (int64_t)c * Mf);
             }
@@ -383,6 +385,11 @@ spread_kernel(const SpreadParams<R> p) {
             }
             const int64_t off = (int64_t)(org[0] + l0) + (int64_t)(org[1] + l1) * g.gs1 +
                                 (int64_t)(org[2] + l2) * g.gs2;
+            // the cells this lane writes: gi (if in0) and gi + 1 (if in1)
+            const int64_t gi = ((int64_t)f * p.coils + c0 + coil) * g.gsp + off;
+            if ((in0 || in1) &&
+                !GBN_INB(g.check, gi + (in0 ? 0 : 1) >= 0 && gi + (in1 ? 1 : 0) < g.grid_elems, CHK_GRID_WRITE))
+                continue;
             C* dst = p.grid + ((int64_t)f * p.coils + c0 + coil) * g.gsp + off;
             if (in0 && in1 && vec_ok) {
                 store_pair(dst, v0, v1);
@@ -392,7 +399,11 @@ spread_kernel(const SpreadParams<R> p) {
             }
         } else {
             const int cell = l0 + Td[0] * (l1 + Td[1] * l2);
-            C* dst = p.scratch + (((int64_t)slot_id * gridDim.y + blockIdx.y) * LS + coil) * p.tile_cells + cell;
+            const int64_t si = (((int64_t)slot_id * gridDim.y + blockIdx.y) * LS + coil) * p.tile_cells + cell;
+            if ((in0 || in1) &&
+                !GBN_INB(g.check, si + (in0 ? 0 : 1) >= 0 && si + (in1 ? 1 : 0) < p.scratch_elems, CHK_SCRATCH))
+                continue;
+            C* dst = p.scratch + si;
             if (in0) dst[0] = v0;
             if (in1) dst[1] = v1;
         }
@@ -436,7 +447,11 @@ __global__ void __launch_bounds__(256) reduce_kernel(const ReduceParams<R> p, co
     for (int d = 0; d < NDIM; ++d) inside = inside && (r[d] < ext[d]);
     if (!inside) return;
     const int64_t pstride = (int64_t)gridDim.y * LS * p.tile_cells;
-    const C* src = p.scratch + (((int64_t)slot0 * gridDim.y + blockIdx.y) * LS + c) * p.tile_cells + cell;
+    const int64_t s0 = (((int64_t)slot0 * gridDim.y + blockIdx.y) * LS + c) * p.tile_cells + cell;
+    if (!GBN_INB(g.check, slot0 >= 0 && nparts >= 1 && s0 + (int64_t)(nparts - 1) * pstride < p.scratch_elems,
+                 CHK_SCRATCH))
+        return;
+    const C* src = p.scratch + s0;
     C acc = cmake<R>((R)0, (R)0);
     int s = 0;
     for (; s + 4 <= nparts; s += 4) {
@@ -459,7 +474,8 @@ __global__ void __launch_bounds__(256) reduce_kernel(const ReduceParams<R> p, co
     for (int d = 0; d < NDIM; ++d) k[d] = org[d] + r[d];
     const int64_t off = k[0] + (int64_t)k[1] * g.gs1 + (int64_t)k[2] * g.gs2;
     if (p.apply_pb) acc = cmulc(acc, phase_before(g, k));
-    p.grid[((int64_t)f * p.coils + c0 + c) * g.gsp + off] = acc;
+    const int64_t gi = ((int64_t)f * p.coils + c0 + c) * g.gsp + off;
+    if (GBN_INB(g.check, gi >= 0 && gi < g.grid_elems, CHK_GRID_WRITE)) p.grid[gi] = acc;
 }
 
 template <typename R>

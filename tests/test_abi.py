@@ -112,3 +112,20 @@ def test_null_arguments_are_rejected(lib):
     assert lib.gbn_dtft_forward(0, nd, sh, None, 1, None, None, 1, None) == 1
     assert lib.gbn_dtft_forward(2, nd, sh, None, 5, None, None, 1, None) == 1
     assert lib.gbn_version().startswith(b"gbnufft")
+
+
+def test_checked_build_exports_every_declared_symbol():
+    """The bounds-checked build (GBN_CHECKED) exposes the same C ABI."""
+    from mrrt.nufft_gb300 import _build
+
+    path = _build.build(checked=True)
+    out = subprocess.run(["nm", "-D", "--defined-only", path], capture_output=True, text=True,
+                         check=True).stdout
+    exported = set(re.findall(r"\bT (gbn_[a-z0-9_]+)", out))
+    missing = [n for n in declared_functions() if n not in exported]
+    assert not missing, missing
+
+
+def test_check_status_rejects_a_null_plan(lib):
+    status = ctypes.c_uint(7)
+    assert lib.gbn_debug_check_status(None, ctypes.byref(status)) == 1   # GBN_ERR_INVALID
