@@ -930,6 +930,23 @@ def run_profile(args):
         print(json.dumps({"profile_case": w["name"], "coils": C, "samples": S.M_total,
                           "stats": S.plan.stats()}))
         return
+    if w["kind"] == "grad2d":
+        # one differentiable step: forward, backward (image and omega
+        # gradients), then a moved trajectory re-binned on the device
+        from mrrt.nufft_gb300.autograd import NufftOperator
+        from mrrt.nufft_gb300.trajectories import spiral_2d
+
+        om0 = spiral_2d(w["interleaves"], w["samples"])
+        op = NufftOperator(w["Nd"], om0, Jd=w["Jd"], Kd=w["Kd"], Ld=w["L"], max_coils=C)
+        dev = op.device
+        om = torch.from_numpy(om0.astype(np.float32)).to(dev)
+        x = torch.randn((C,) + tuple(w["Nd"]), dtype=torch.complex64, device=dev).requires_grad_(True)
+        for k in range(args.warmup + args.steps):
+            o = (om + 1e-3 * (k % 2)).requires_grad_(True)
+            op.forward(x, o).abs().pow(2).sum().backward()
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_case": w["name"], "coils": C, "samples": op.M, "stats": op.plan.stats()}))
+        return
     omega, x_f = build_inputs()
     A = NufftBase(Nd=w["Nd"], omega=omega, Jd=w["Jd"], Kd=w["Kd"], Ld=w["L"], precision="single",
                   on_gpu=True, max_coils=C)

@@ -126,9 +126,15 @@ __global__ void __launch_bounds__(256) bin_emit_kernel(const BinParams<R> p) {
             }
 }
 
+// Counts per bin of sorted keys: lanes holding the same key (a run of the
+// sort) add once, through their lowest lane.
 __global__ void __launch_bounds__(256) bin_hist_kernel(const unsigned* keys, int64_t n, int* counts) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) atomicAdd(&counts[keys[i]], 1);
+    const unsigned lane = threadIdx.x & 31;
+    const bool ok = i < n;
+    const unsigned k = ok ? keys[i] : 0xffffffffu;
+    const unsigned peers = __match_any_sync(0xffffffffu, k);
+    if (ok && (peers & ((1u << lane) - 1u)) == 0) atomicAdd(&counts[k], __popc(peers));
 }
 
 // parts per bin: gather chunks (none for an empty tile), spread parts (at

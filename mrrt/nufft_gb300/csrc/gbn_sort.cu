@@ -17,9 +17,12 @@ constexpr int SCAN_TILE = SCAN_THREADS * SCAN_PER_THREAD;   // 2048 elements per
 
 constexpr int RADIX_THREADS = 256;
 constexpr int RADIX_WARPS = RADIX_THREADS / 32;
-constexpr int RADIX_ROUNDS = 16;                            // items per lane
-constexpr int RADIX_TILE = RADIX_THREADS * RADIX_ROUNDS;    // 4096 items per CTA
 constexpr int RADIX_BUCKETS = 256;
+// Items per lane: 16 (4096 items per CTA) for large sorts; 2 (512 per CTA)
+// below RADIX_SMALL items, where 4096-item tiles would leave most SMs idle.
+constexpr int RADIX_ROUNDS_LARGE = 16, RADIX_ROUNDS_SMALL = 2;
+constexpr int64_t RADIX_SMALL = 1 << 20;
+inline int radix_rounds(int64_t n) { return n < RADIX_SMALL ? RADIX_ROUNDS_SMALL : RADIX_ROUNDS_LARGE; }
 
 inline size_t round256(size_t v) { return (v + 255) & ~(size_t)255; }
 
@@ -85,8 +88,10 @@ __global__ void scan_total_kernel(const int* in, const int* out, int64_t n, int*
 
 __device__ __forceinline__ int digit_of(unsigned key, int shift) { return (int)((key >> shift) & 0xffu); }
 
+template <int RADIX_ROUNDS>
 __global__ void __launch_bounds__(RADIX_THREADS) radix_hist_kernel(const unsigned* keys, int64_t n, int shift,
                                                                    int nblk, int* hist) {
+    constexpr int RADIX_TILE = RADIX_THREADS * RADIX_ROUNDS;
     __shared__ int h[RADIX_BUCKETS];
     for (int q = threadIdx.x; q < RADIX_BUCKETS; q += blockDim.x) h[q] = 0;
     __syncthreads();
@@ -105,10 +110,12 @@ __global__ void __launch_bounds__(RADIX_THREADS) radix_hist_kernel(const unsigne
 
 // Items of a CTA in index order are (warp, round, lane); each lands after
 // every earlier item with the same digit, so the pass is stable.
+template <int RADIX_ROUNDS>
 __global__ void __launch_bounds__(RADIX_THREADS) radix_scatter_kernel(const unsigned* keys, const unsigned* vals,
                                                                       int64_t n, int shift, int nblk,
                                                                       const int* offs, unsigned* keys_out,
                                                                       unsigned* vals_out) {
+    constexpr int RADIX_TILE = RADIX_THREADS * RADIX_ROUNDS;
     __shared__ int wh[RADIX_WARPS][RADIX_BUCKETS];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     for (int q = lane; q < RADIX_BUCKETS; q += 32) wh[warp][q] = 0;
@@ -194,7 +201,9 @@ cudaError_t exclusive_scan(const int* in, int* out, int64_t n, int* total, void*
 // temp layout: keys and values of the other ping-pong side, the digit
 // histogram, its scan, the scan's own temporaries (each 256-byte aligned)
 size_t radix_temp_bytes(int64_t n) {
-    const int64_t nblk = (n + RADIX_TILE - 1) / RADIX_TILE;
+    // the larger of the two tilings' histograms (either may run for a
+    // smaller sort sharing this workspace)
+    const int64_t nblk = (n + RADIX_THREADS * RADIX_ROUNDS_SMALL - 1) / (RADIX_THREADS * RADIX_ROUNDS_SMALL);
     const int64_t nh = nblk * RADIX_BUCKETS;
     return 2 * round256((size_t)n * sizeof(unsigned)) + 2 * round256((size_t)nh * sizeof(int)) +
            scan_temp_bytes(nh);
@@ -202,7 +211,9 @@ size_t radix_temp_bytes(int64_t n) {
 
 cudaError_t radix_sort_pairs(unsigned* keys, unsigned* vals, int64_t n, int bits, void* temp, cudaStream_t s) {
     if (n <= 1 || bits <= 0) return cudaSuccess;
-    const int nblk = (int)((n + RADIX_TILE - 1) / RADIX_TILE);
+    const int rounds = radix_rounds(n);
+    const int tile = RADIX_THREADS * rounds;
+    const int nblk = (int)((n + tile - 1) / tile);
     const int64_t nh = (int64_t)nblk * RADIX_BUCKETS;
     char* t = reinterpret_cast<char*>(temp);
     unsigned* k2 = reinterpret_cast<unsigned*>(t);
@@ -217,10 +228,16 @@ cudaError_t radix_sort_pairs(unsigned* keys, unsigned* vals, int64_t n, int bits
     unsigned *ka = keys, *va = vals, *kb = k2, *vb = v2;
     int passes = 0;
     for (int shift = 0; shift < bits; shift += 8, ++passes) {
-        radix_hist_kernel<<<nblk, RADIX_THREADS, 0, s>>>(ka, n, shift, nblk, hist);
+        if (rounds == RADIX_ROUNDS_SMALL)
+            radix_hist_kernel<RADIX_ROUNDS_SMALL><<<nblk, RADIX_THREADS, 0, s>>>(ka, n, shift, nblk, hist);
+        else
+            radix_hist_kernel<RADIX_ROUNDS_LARGE><<<nblk, RADIX_THREADS, 0, s>>>(ka, n, shift, nblk, hist);
         cudaError_t e = exclusive_scan(hist, offs, nh, nullptr, stmp, s);
         if (e != cudaSuccess) return e;
-        radix_scatter_kernel<<<nblk, RADIX_THREADS, 0, s>>>(ka, va, n, shift, nblk, offs, kb, vb);
+        if (rounds == RADIX_ROUNDS_SMALL)
+            radix_scatter_kernel<RADIX_ROUNDS_SMALL><<<nblk, RADIX_THREADS, 0, s>>>(ka, va, n, shift, nblk, offs, kb, vb);
+        else
+            radix_scatter_kernel<RADIX_ROUNDS_LARGE><<<nblk, RADIX_THREADS, 0, s>>>(ka, va, n, shift, nblk, offs, kb, vb);
         unsigned* tk = ka; ka = kb; kb = tk;
         unsigned* tv = va; va = vb; vb = tv;
     }
