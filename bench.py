@@ -48,6 +48,9 @@ WORKLOADS = {
     "2d-multicoil-radial": dict(name="2d-multicoil-radial", kind="radial2d", Nd=(256, 256),
                                 Kd=(512, 512), Jd=(6, 6), L=1024, spokes=402, readout=512, coils=32),
     # 3-D kooshball: interp3 gather and 3-D tiled spread
+    # the reference's CPU-runnable case: 128^2 image, 128 uniformly spaced spokes x 256, one coil
+    "2d-radial-128": dict(name="2d-radial-128", kind="radial2d", Nd=(128, 128), Kd=(256, 256), Jd=(6, 6),
+                          L=1024, spokes=128, readout=256, coils=1, golden=False),
     "3d-kooshball": dict(name="3d-kooshball", kind="koosh3d", Nd=(128, 128, 128), Kd=(256, 256, 256),
                          Jd=(6, 6, 6), L=1024, spokes=12000, readout=256, coils=8),
     # the 3-D kernels on a smaller volume (inputs still larger than L2), for profiler captures
@@ -72,7 +75,7 @@ def build_inputs():
     if w["kind"] == "koosh3d":
         omega = kooshball_3d(w["spokes"], w["readout"])
     else:
-        omega = radial_2d(w["spokes"], w["readout"], golden=True)
+        omega = radial_2d(w["spokes"], w["readout"], golden=w.get("golden", True))
     img = complex_image(w["Nd"], seed=0).astype(np.complex128)
     maps = gaussian_coil_maps(w["Nd"], w["coils"])
     x = (maps * img[None]).astype(np.complex64)           # [C, *Nd]
@@ -330,7 +333,8 @@ def config_dict(extra=None):
            "L": w["L"], "coils": w["coils"], "precision": "single",
            "l2": "flushed between timed steps (256 MB write)", "parallelism": "replicas"}
     if w["kind"] == "radial2d":
-        cfg["trajectory"] = "golden-angle radial %dx%d" % (w["spokes"], w["readout"])
+        cfg["trajectory"] = "%s radial %dx%d" % ("golden-angle" if w.get("golden", True) else "uniform-angle",
+                                                  w["spokes"], w["readout"])
         cfg["samples"] = w["spokes"] * w["readout"]
     elif w["kind"] == "koosh3d":
         cfg["trajectory"] = "kooshball %d spokes x %d on a Fibonacci sphere" % (w["spokes"], w["readout"])
