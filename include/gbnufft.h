@@ -5,6 +5,11 @@
  * returns a status code (GBN_OK on success); gbn_last_error() describes the
  * most recent failure on the calling thread.  No entry point aborts.
  *
+ * A plan owns device working storage (the oversampled grid, the partial sums
+ * of split tiles, the work counters of the 3-D interpolation launch): the
+ * calls on one plan must not overlap in time.  Issue them on one stream, or
+ * synchronise between streams; separate plans may run concurrently.
+ *
  * Axis convention.  The plan is described in MEMORY-AXIS order: axis 0 is
  * the fastest-varying index of the image and of the oversampled grid.  A
  * Fortran-ordered numpy image of shape Nd (the reference's layout,

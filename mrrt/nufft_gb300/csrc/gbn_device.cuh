@@ -191,6 +191,28 @@ __device__ __forceinline__ void qfma(C& acc, C c, C v) {
 }
 
 
+// Work distribution of the persistent interpolation kernels.  tickets[0]
+// hands out (work item, coil chunk) pairs in item order (items are sorted
+// heaviest first); tickets[1] counts the CTAs that found no more work, and
+// the last of them resets both to zero for the next launch (stream-ordered,
+// so graph replays work too).  Nothing waits on another CTA.
+__device__ __forceinline__ int next_ticket(int* tickets, int* slot) {
+    if (threadIdx.x == 0) *slot = atomicAdd(&tickets[0], 1);
+    __syncthreads();
+    const int t = *slot;
+    __syncthreads();   // every thread has its ticket before thread 0 takes the next
+    return t;
+}
+__device__ __forceinline__ void retire_ctas(int* tickets) {
+    if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(&tickets[1], 1) == (int)gridDim.x - 1) {
+            tickets[0] = 0;
+            tickets[1] = 0;
+        }
+    }
+}
+
 // Two adjacent complex values in one 16-byte store (single precision; the
 // address must be 16-byte aligned).  Double precision stores them singly.
 __device__ __forceinline__ void store_pair(float2* dst, float2 a, float2 b) {

@@ -110,6 +110,9 @@ struct GatherParams {
     int apply_pb;                   // multiply staged cells by phase_before
     R grid_scale;                   // divide staged cells by this (ortho)
     int apply_ph;                   // multiply outputs by the sample phase
+    int* tickets;                   // work counter pair of the persistent (3-D) launch, zero
+                                    // between launches; the 1-D and 2-D kernels ignore it
+    int chunks;                     // coil chunks of LS lanes
 };
 
 template <typename R>
@@ -129,6 +132,7 @@ struct SpreadParams {
     int64_t scratch_elems;          // scratch extent (complex elements)
     int apply_pb;
     int apply_ph;
+    int chunks;                     // coil chunks of LS lanes (gridDim.y)
 };
 
 template <typename R>
@@ -293,6 +297,11 @@ int spread_threads(int ndim, const int* T);
 // (later launches needing no more skip the call), so launches recorded in a
 // CUDA graph after a warm-up call make no attribute call.
 cudaError_t ensure_dynamic_smem(const void* kernel, size_t bytes);
+
+// CTAs of `kernel` (with this block size and dynamic shared memory) that fit
+// on the current device at once: the grid of a persistent launch.  Cached
+// per (kernel, device, threads, smem); 0 if the query fails.
+int resident_ctas(const void* kernel, int threads, size_t smem);
 
 // Address and size of the fixed no-alloc scratch array on the current device
 // (gbn_noalloc.cu); looked up on every request.

@@ -50,6 +50,26 @@ cudaError_t ensure_dynamic_smem(const void* kernel, size_t bytes) {
     return cudaSuccess;
 }
 
+int resident_ctas(const void* kernel, int threads, size_t smem) {
+    struct Entry { const void* k; int dev, threads; size_t smem; int ctas; };
+    static std::mutex mu;
+    static std::vector<Entry> done;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+    std::lock_guard<std::mutex> lk(mu);
+    for (auto& x : done)
+        if (x.k == kernel && x.dev == dev && x.threads == threads && x.smem == smem) return x.ctas;
+    int per_sm = 0, sms = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    const int ctas = std::max(1, per_sm) * std::max(1, sms);
+    done.push_back({kernel, dev, threads, smem, ctas});
+    return ctas;
+}
+
 }  // namespace gbn
 
 namespace {
@@ -185,6 +205,7 @@ struct gbn_plan {
 
     DevBuf tables, dtables, sn, dfoff;
     DevBuf check;         // status word of the checked build's bounds tests
+    DevBuf tickets;       // work counters of the persistent gather launch
     DevBuf weights;       // sparse-matrix mode: per-axis [M_total][J] weights (re, then im)
     DevBuf gcoef, scoef;  // precomputed coefficients in gather / spread list order
     bool coefs = false;   // gcoef / scoef hold the current lists' coefficients
@@ -851,6 +872,9 @@ int run_gather(gbn_plan* P, const void* grid, void* y, int coils, bool phases, c
     p.apply_ph = phases && P->has_phase;
     p.g.grid_elems = (int64_t)P->F * coils * P->Kprod;
     p.g.sample_elems = (int64_t)coils * P->M_total;
+    // work counters of the persistent (3-D) gather launch; unused in 1-D, 2-D
+    p.tickets = reinterpret_cast<int*>(P->tickets.p);
+    p.chunks = (coils + p.ln.LS - 1) / p.ln.LS;
     GBN_CUDA(launch_gather<R>(p, s), "gather launch");
     return GBN_OK;
 }
@@ -876,6 +900,7 @@ int run_spread(gbn_plan* P, const void* y, void* grid, int coils, bool phases, c
     p.scratch = reinterpret_cast<C*>(P->scratch.p);
     p.tile_cells = (int64_t)P->Ts[0] * P->Ts[1] * P->Ts[2];
     p.scratch_elems = P->scratch_cap;
+    p.chunks = (coils + p.ln.LS - 1) / p.ln.LS;
     p.g.grid_elems = (int64_t)P->F * coils * P->Kprod;
     p.g.sample_elems = (int64_t)coils * P->M_total;
     p.apply_pb = phases && P->geom.phasing == GBN_PHASING_REAL;
@@ -937,6 +962,7 @@ int run_spread_noalloc(gbn_plan* P, const void* y, void* grid, int coils, cudaSt
     p.scratch = reinterpret_cast<C*>(scratch);
     p.tile_cells = tile_cells;
     p.scratch_elems = (int64_t)(cap / sizeof(C));
+    p.chunks = (coils + ln.LS - 1) / ln.LS;
     p.g.grid_elems = (int64_t)P->F * coils * P->Kprod;
     p.g.sample_elems = (int64_t)coils * P->M_total;
     p.apply_pb = 0;
@@ -1613,6 +1639,8 @@ int gbn_plan_create(gbn_plan** out, const gbn_geometry* geom, const void* const*
     {
         cudaError_t e = P->check.alloc(16);
         if (e == cudaSuccess) e = cudaMemset(P->check.p, 0, 16);
+        if (e == cudaSuccess) e = P->tickets.alloc(16);
+        if (e == cudaSuccess) e = cudaMemset(P->tickets.p, 0, 16);
         if (e != cudaSuccess) {
             delete P;
             return cuda_fail(e, "status word");

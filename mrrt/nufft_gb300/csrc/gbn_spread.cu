@@ -148,11 +148,16 @@ spread_kernel(const SpreadParams<R> p) {
     short4* lsb = reinterpret_cast<short4*>(cp + CH * SL::PSTR);
     R* tb = reinterpret_cast<R*>(lsb + 2 * CH);
 
-    const int4 it = p.items[blockIdx.x];
-    const int2 part = p.parts[blockIdx.x];
+    // One CTA per (work item, coil chunk).  (A persistent launch, resident
+    // CTAs taking work tickets as the 3-D gather does, measured slower here:
+    // 0.191 against 0.151 ms at the 2-D 32-coil workload, 5.78 against
+    // 5.71 ms at the 3-D kooshball.)
+    const int item = blockIdx.x, chunk = blockIdx.y;
+    const int4 it = p.items[item];
+    const int2 part = p.parts[item];
     const int f = it.x, tile = it.y, start = it.z, count = it.w;
     if (!GBN_INB(g.check, start >= 0 && count >= 0 && start + (int64_t)count <= p.s.len, CHK_LIST)) return;
-    const int c0 = blockIdx.y << lsh;
+    const int c0 = chunk << lsh;
     const int nc = min(LS, p.coils - c0);
 
     int org[3] = {0, 0, 0}, ext[3] = {1, 1, 1}, Td[3] = {1, 1, 1};
@@ -183,10 +188,11 @@ spread_kernel(const SpreadParams<R> p) {
     const C* yb = p.y + fo * p.coils + (int64_t)c0 * Mf;
 
     // zero padding of the coefficient rows: written once, the J coefficient
-    // slots of each row are overwritten per chunk
-    // (an empty tile -- no entry touches it -- needs no rows: it only writes zeros)
-    if (count > 0)
-        for (int q = tid; q < CH * SL::PSTR; q += blockDim.x) cp[q] = cmake<R>((R)0, (R)0);
+    // slots of each row are overwritten per chunk.  Only the rows of entries
+    // the item has are ever read (a tile of 25 entries zeroes 25 rows, not
+    // 64); an empty tile -- no entry touches it -- needs none: it only writes
+    // zeros
+    for (int q = tid; q < min(count, CH) * SL::PSTR; q += blockDim.x) cp[q] = cmake<R>((R)0, (R)0);
     const int Jsum = Jx + (NDIM > 1 ? Jy : 0) + (NDIM > 2 ? Jz : 0);
 
     // Copy-in assignment: each thread owns up to two entries of a chunk and
@@ -399,7 +405,7 @@ spread_kernel(const SpreadParams<R> p) {
             }
         } else {
             const int cell = l0 + Td[0] * (l1 + Td[1] * l2);
-            const int64_t si = (((int64_t)slot_id * gridDim.y + blockIdx.y) * LS + coil) * p.tile_cells + cell;
+            const int64_t si = (((int64_t)slot_id * p.chunks + chunk) * LS + coil) * p.tile_cells + cell;
             if ((in0 || in1) &&
                 !GBN_INB(g.check, si + (in0 ? 0 : 1) >= 0 && si + (in1 ? 1 : 0) < p.scratch_elems, CHK_SCRATCH))
                 continue;
@@ -502,8 +508,8 @@ static cudaError_t spread_launch(const SpreadParams<R>& p, cudaStream_t s) {
     if (e != cudaSuccess) return e;
     const int threads = spread_threads(NDIM, p.g.T);
     if (threads < 32 || threads > 256) return cudaErrorInvalidConfiguration;
-    dim3 grid(p.nitems, (p.coils + p.ln.LS - 1) / p.ln.LS);
-    spread_kernel<R, NDIM, CX, JJ, LSC, ROWSKIP><<<grid, threads, smem, s>>>(p);
+    if (p.chunks != (p.coils + p.ln.LS - 1) / p.ln.LS) return cudaErrorInvalidValue;
+    spread_kernel<R, NDIM, CX, JJ, LSC, ROWSKIP><<<dim3(p.nitems, p.chunks), threads, smem, s>>>(p);
     return cudaGetLastError();
 }
 
