@@ -19,6 +19,7 @@ GBN_ERR_UNSUPPORTED = 5
 GBN_ERR_TOOLARGE = 6
 
 FLAG_TABLE_ONLY = 1
+FLAG_CUFFT_ONLY = 2
 
 PRECISION = {"single": 0, "double": 1}
 PHASING = {"real": 0, "complex": 1}

@@ -40,7 +40,7 @@ class GpuPlan:
     def __init__(self, Nd, Kd, Jd, L, rdt, tables_re, tables_im, sn, tm, sample_phase,
                  frame_offsets=None, ortho=False, adjoint_scale=1.0, pb_coef=None, pb_order=None,
                  phasing="real", max_coils=1, tile=None, stile=None, device=None, table_only=False,
-                 lib=None):
+                 cufft_only=False, lib=None):
         require_cuda()
         # lib: a loaded libgbnufft (default); _lib.load_checked() gives the
         # bounds-checked build
@@ -64,7 +64,7 @@ class GpuPlan:
         g.adjoint_scale = float(adjoint_scale)
         g.n_frames = 1 if frame_offsets is None else len(frame_offsets) - 1
         g.max_coils = max(1, int(max_coils))
-        g.flags = _lib.FLAG_TABLE_ONLY if table_only else 0
+        g.flags = (_lib.FLAG_TABLE_ONLY if table_only else 0) | (_lib.FLAG_CUFFT_ONLY if cufft_only else 0)
         self.geom = g
         self._keep = []
         hre = [np.ascontiguousarray(t, dtype=self.rdt) for t in tables_re]

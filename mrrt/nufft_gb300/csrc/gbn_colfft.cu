@@ -1,0 +1,248 @@
+// Pruned FFT pass along the slowest axis of the oversampled grid.
+//
+// The oversampled FFT (mrrt/nufft/_nufft.py:1330-1350 forward fftn of the
+// zero-padded image, :1561-1572 adjoint ifftn before the crop) is done in
+// passes.  Its last pass runs along the slowest memory axis (axis 1 in 2-D,
+// axis 2 in 3-D): an [L][S] array -- S columns, row stride S -- transformed
+// along L for every column, for one or several planes at a plane stride.
+// Half of that axis is zero padding:
+//   * forward, only the first nin = N_last rows hold data; rows past nin are
+//     zero and are not read;
+//   * inverse, only the first nout = N_last rows are used afterwards (the
+//     crop reads them); the others are not written.
+// cuFFT reads and writes all L rows; this pass moves 3/4 of that traffic.
+//
+// Algorithm: the four-step split L = L1 L2 of the Cooley-Tukey FFT,
+//   X[k2 + L2 k1] = sum_n1 W_L1^(n1 k1) W_L^(n1 k2) sum_n2 x[n1 + L1 n2] W_L2^(n2 k2),
+// with W_M = exp(-2 pi i / M) forward and its conjugate inverse.
+//   step A: a thread per (column, n1) loads the L2 rows n1 + L1 n2 of its
+//     column (16 or 8 adjacent columns per CTA: 128- or 64-byte row segments), transforms
+//     them in registers, multiplies by W_L^(n1 k2) and stores to shared memory;
+//   step B: a thread per (column, k2) reads its L1 values back, transforms
+//     them in registers and stores rows k2 + L2 k1.
+// The register transforms are Stockham autosort FFTs (Govindaraju et al.,
+// "High performance discrete Fourier transforms on graphics processors",
+// SC 2008), radix 4, 2 and 3 stages fully unrolled; their roots are compile-
+// time constants in constant memory, the W_L^(n1 k2) twiddles a per-plan
+// table computed on the host in double precision.  Single precision only;
+// other lengths and double precision run the pass through cuFFT.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "gbn_device.cuh"
+#include "gbn_internal.h"
+
+namespace gbn {
+
+namespace {
+
+// Columns per CTA: 16 (128-byte row segments), 8 for 32-point second
+// stages (a 256-thread CTA, so that the 32-point transforms need no spills).
+constexpr int cf_tc(int L1) { return L1 >= 32 ? 8 : 16; }
+
+// exp(-2 pi i m / 96), m < 96: the roots of every register transform (its
+// length divides 96).  cos and sin by their Taylor series on [-pi, pi]
+// (30 terms, error far below float rounding), evaluated by the compiler.
+constexpr double kPi = 3.14159265358979323846;
+constexpr double reduce_angle(int m) { return 2 * kPi * m / 96 > kPi ? 2 * kPi * m / 96 - 2 * kPi : 2 * kPi * m / 96; }
+constexpr double series_cos(double x) {
+    double t = 1, s = 1;
+    for (int k = 1; k < 30; ++k) {
+        t *= -x * x / ((2.0 * k - 1) * (2.0 * k));
+        s += t;
+    }
+    return s;
+}
+constexpr double series_sin(double x) {
+    double t = x, s = x;
+    for (int k = 1; k < 30; ++k) {
+        t *= -x * x / ((2.0 * k) * (2.0 * k + 1));
+        s += t;
+    }
+    return s;
+}
+#define GBN_ROOT(m) {(float)series_cos(reduce_angle(m)), (float)-series_sin(reduce_angle(m))}
+#define GBN_ROOT4(m) GBN_ROOT(m), GBN_ROOT(m + 1), GBN_ROOT(m + 2), GBN_ROOT(m + 3)
+#define GBN_ROOT16(m) GBN_ROOT4(m), GBN_ROOT4(m + 4), GBN_ROOT4(m + 8), GBN_ROOT4(m + 12)
+__constant__ float2 c_root96[96] = {GBN_ROOT16(0), GBN_ROOT16(16), GBN_ROOT16(32),
+                                    GBN_ROOT16(48), GBN_ROOT16(64), GBN_ROOT16(80)};
+#undef GBN_ROOT16
+#undef GBN_ROOT4
+#undef GBN_ROOT
+
+__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+// multiply by i^(SIGN), i.e. -i forward, +i inverse
+template <int SIGN>
+__device__ __forceinline__ float2 mul_si(float2 a) { return SIGN < 0 ? make_float2(a.y, -a.x) : make_float2(-a.y, a.x); }
+
+// v * (root m of 96, conjugated for the inverse); m is a compile-time value
+// once the loops are unrolled, so the quarter turns cost no multiply.
+template <int SIGN>
+__device__ __forceinline__ float2 root_mul(float2 v, int m) {
+    if (m == 0) return v;
+    if (m == 48) return make_float2(-v.x, -v.y);
+    if (m == 24) return mul_si<SIGN>(v);
+    if (m == 72) return mul_si<-SIGN>(v);
+    float2 w = c_root96[m];
+    if (SIGN > 0) w.y = -w.y;
+    return cmul(v, w);
+}
+
+template <int R, int SIGN>
+__device__ __forceinline__ void butterfly(float2 (&v)[R]) {
+    if constexpr (R == 2) {
+        const float2 a = v[0];
+        v[0] = cadd(a, v[1]);
+        v[1] = csub(a, v[1]);
+    } else if constexpr (R == 4) {
+        const float2 t0 = cadd(v[0], v[2]), t1 = csub(v[0], v[2]);
+        const float2 t2 = cadd(v[1], v[3]), t3 = mul_si<SIGN>(csub(v[1], v[3]));
+        v[0] = cadd(t0, t2);
+        v[2] = csub(t0, t2);
+        v[1] = cadd(t1, t3);
+        v[3] = csub(t1, t3);
+    } else {
+        static_assert(R == 3, "radix 2, 3 or 4");
+        // w = exp(SIGN 2 pi i / 3) = -1/2 + SIGN i sqrt(3)/2
+        constexpr float h = 0.866025403784438646763723f;   // sqrt(3) / 2
+        const float2 t = cadd(v[1], v[2]);
+        const float2 d = csub(v[1], v[2]);
+        const float2 u = SIGN < 0 ? make_float2(h * d.y, -h * d.x) : make_float2(-h * d.y, h * d.x);
+        const float2 m = make_float2(v[0].x - 0.5f * t.x, v[0].y - 0.5f * t.y);
+        v[0] = cadd(v[0], t);
+        v[1] = cadd(m, u);
+        v[2] = csub(m, u);
+    }
+}
+
+constexpr int stage_radix(int n) { return n % 4 == 0 ? 4 : (n % 2 == 0 ? 2 : 3); }
+
+// In-register Stockham FFT of length N (N divides 96), stages of NS -> NS R.
+template <int N, int NS, int SIGN>
+__device__ __forceinline__ void stockham(float2 (&x)[N]) {
+    if constexpr (NS < N) {
+        constexpr int R = stage_radix(N / NS);
+        constexpr int Q = N / R;
+        static_assert(96 % (NS * R) == 0, "register transform lengths divide 96");
+        float2 y[N];
+#pragma unroll
+        for (int j = 0; j < Q; ++j) {
+            const int jm = j % NS;
+            float2 v[R];
+#pragma unroll
+            for (int r = 0; r < R; ++r) v[r] = x[j + r * Q];
+#pragma unroll
+            for (int r = 1; r < R; ++r) v[r] = root_mul<SIGN>(v[r], jm * r * (96 / (NS * R)));
+            butterfly<R, SIGN>(v);
+            const int base = (j / NS) * NS * R + jm;
+#pragma unroll
+            for (int r = 0; r < R; ++r) y[base + r * NS] = v[r];
+        }
+#pragma unroll
+        for (int i = 0; i < N; ++i) x[i] = y[i];
+        stockham<N, NS * R, SIGN>(x);
+    }
+}
+
+template <int L1, int L2, int CF_TC, int SIGN>
+__global__ void __launch_bounds__(CF_TC * L1) colfft_kernel(const ColFftParams p) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float2* sm = reinterpret_cast<float2*>(smem_raw);
+    const int64_t c0 = (int64_t)blockIdx.x * CF_TC;
+    const int64_t pb = (int64_t)blockIdx.y * p.ps;
+
+    // step A: (column, n1), L2-point transforms of rows n1 + L1 n2
+    {
+        const int col = threadIdx.x % CF_TC, n1 = threadIdx.x / CF_TC;
+        const int64_t c = c0 + col;
+        float2 v[L2];
+#pragma unroll
+        for (int n2 = 0; n2 < L2; ++n2) {
+            const int n = n1 + L1 * n2;
+            const int64_t i = pb + (int64_t)n * p.S + c;
+            v[n2] = make_float2(0.f, 0.f);
+            if (n < p.nin && c < p.S && GBN_INB(p.check, i >= 0 && i < p.in_elems, CHK_GRID_READ)) v[n2] = p.in[i];
+        }
+        stockham<L2, 1, SIGN>(v);
+#pragma unroll
+        for (int k2 = 1; k2 < L2; ++k2) {
+            float2 w = __ldg(p.tw + n1 * k2);   // n1 k2 < L
+            if (SIGN > 0) w.y = -w.y;
+            v[k2] = cmul(v[k2], w);
+        }
+#pragma unroll
+        for (int k2 = 0; k2 < L2; ++k2) sm[(k2 * L1 + n1) * CF_TC + col] = v[k2];
+    }
+    __syncthreads();
+    // step B: (column, k2), L1-point transforms, rows k2 + L2 k1 out
+    for (int q = threadIdx.x; q < CF_TC * L2; q += CF_TC * L1) {
+        const int col = q % CF_TC, k2 = q / CF_TC;
+        const int64_t c = c0 + col;
+        float2 u[L1];
+#pragma unroll
+        for (int n1 = 0; n1 < L1; ++n1) u[n1] = sm[(k2 * L1 + n1) * CF_TC + col];
+        stockham<L1, 1, SIGN>(u);
+#pragma unroll
+        for (int k1 = 0; k1 < L1; ++k1) {
+            const int k = k2 + L2 * k1;
+            const int64_t i = pb + (int64_t)k * p.S + c;
+            if (k < p.nout && c < p.S && GBN_INB(p.check, i >= 0 && i < p.out_elems, CHK_GRID_WRITE)) p.out[i] = u[k1];
+        }
+    }
+}
+
+template <int L1, int L2, int CF_TC = cf_tc(L1)>
+cudaError_t colfft_launch(const ColFftParams& p, int sign, cudaStream_t s) {
+    constexpr int L = L1 * L2;
+    const size_t smem = (size_t)CF_TC * L * sizeof(float2);
+    const void* k = sign < 0 ? reinterpret_cast<const void*>(colfft_kernel<L1, L2, CF_TC, -1>)
+                             : reinterpret_cast<const void*>(colfft_kernel<L1, L2, CF_TC, 1>);
+    cudaError_t e = ensure_dynamic_smem(k, smem);
+    if (e != cudaSuccess) return e;
+    const int64_t ctas = (p.S + CF_TC - 1) / CF_TC;
+    if (ctas > INT32_MAX || p.planes > 65535) return cudaErrorInvalidValue;
+    const dim3 grid((unsigned)ctas, (unsigned)p.planes);
+    if (sign < 0)
+        colfft_kernel<L1, L2, CF_TC, -1><<<grid, CF_TC * L1, smem, s>>>(p);
+    else
+        colfft_kernel<L1, L2, CF_TC, 1><<<grid, CF_TC * L1, smem, s>>>(p);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+// Lengths with a compile-time split L1 x L2 (both dividing 96, at most 32).
+bool colfft_supported(int L) {
+    switch (L) {
+        case 64: case 96: case 128: case 192: case 256: case 384: case 512: case 768: case 1024:
+            return true;
+        default:
+            return false;
+    }
+}
+
+cudaError_t launch_colfft(const ColFftParams& p, int sign, cudaStream_t s) {
+    if (p.S <= 0 || p.planes <= 0 || p.nin < 0 || p.nin > p.L || p.nout < 0 || p.nout > p.L)
+        return cudaErrorInvalidValue;
+    // Splits measured on a GB300 (forward + inverse, L2 larger than the data):
+    //   512, 16384 columns: 32 x 16 with 8 columns per CTA 63 us, 16 x 32
+    //     with 16 columns 70 us, cuFFT 64 us;
+    //   384, 196608 columns: 16 x 24 363 us, 24 x 16 367 us, cuFFT 732 us;
+    //   256, 8 planes of 65536 columns: 16 x 16 679 us, 8 x 32 696 us,
+    //     cuFFT 809 us.
+    switch (p.L) {
+        case 64: return colfft_launch<8, 8>(p, sign, s);
+        case 96: return colfft_launch<8, 12>(p, sign, s);
+        case 128: return colfft_launch<16, 8>(p, sign, s);
+        case 192: return colfft_launch<16, 12>(p, sign, s);
+        case 256: return colfft_launch<16, 16>(p, sign, s);
+        case 384: return colfft_launch<16, 24>(p, sign, s);
+        case 512: return colfft_launch<32, 16>(p, sign, s);
+        case 768: return colfft_launch<32, 24>(p, sign, s);
+        case 1024: return colfft_launch<32, 32>(p, sign, s);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+}  // namespace gbn

@@ -1,5 +1,6 @@
 // Internal declarations shared by the host planner (gbn_plan.cu) and the
-// device kernels (gbn_gather.cu, gbn_spread.cu, gbn_padcrop.cu, gbn_grad.cu).
+// device kernels (gbn_gather.cu, gbn_spread.cu, gbn_padcrop.cu, gbn_grad.cu,
+// gbn_colfft.cu, ...).
 #pragma once
 
 #include <cuda_runtime.h>
@@ -277,6 +278,24 @@ cudaError_t launch_bin_items(const ItemParams& p, cudaStream_t s);
 cudaError_t launch_permute_int4(const int4* in, const unsigned* order, int64_t n, int4* out, cudaStream_t s);
 cudaError_t launch_permute_int2(const int2* in, const unsigned* order, int64_t n, int2* out, cudaStream_t s);
 template <typename R> cudaError_t launch_bin_pack(const PackParams<R>& p, cudaStream_t s);
+
+// Pruned FFT pass along the slowest axis (gbn_colfft.cu): `planes` arrays
+// at plane stride ps, each [L][S] (S columns, row stride S); rows >= nin
+// are read as zero, rows >= nout are not written.  in == out is allowed.
+struct ColFftParams {
+    const float2* in;
+    float2* out;
+    int64_t S;                      // columns per plane, and the row stride (elements)
+    int64_t ps;                     // plane stride (elements)
+    int planes;
+    int L, nin, nout;
+    const float2* tw;               // exp(-2 pi i m / L), m < L
+    unsigned* check;                // checked builds: status word and extents
+    int64_t in_elems, out_elems;
+};
+bool colfft_supported(int L);
+// sign -1: forward (exp(-2 pi i nk / L)), +1: inverse (unnormalised)
+cudaError_t launch_colfft(const ColFftParams& p, int sign, cudaStream_t s);
 
 template <typename R> cudaError_t launch_gather(const GatherParams<R>& p, cudaStream_t s);
 template <typename R> cudaError_t launch_spread(const SpreadParams<R>& p, cudaStream_t s);

@@ -154,7 +154,8 @@ struct DevBuf {
 struct FftEntry {
     int planes;
     cufftHandle h;        // full transform (1-D, 3-D)
-    cufftHandle hx, hy;   // 2-D pruned passes: rows holding data, then all columns
+    cufftHandle hx, hy;   // pruned passes: slabs holding data, then the last axis (hy
+                          // only when the plan's own last-axis pass cannot run)
 };
 
 // State of the host-buffer transforms: two copy streams, events, device
@@ -218,6 +219,8 @@ struct gbn_plan {
     DevBuf mid;           // output of the forward's slab pass (2-D rows, 3-D z-planes); the
                           // slabs >= N_last the last-axis pass reads stay zero
     int64_t mid_clean = 0;     // 2-D: slabs from which mid is known to be zero
+    bool colfft = false;       // last-axis pass by gbn_colfft.cu (else cuFFT)
+    DevBuf colfft_tw;          // its twiddles exp(-2 pi i m / K_last), m < K_last
     int mid_planes = 0;        // planes the mid buffer holds
     int cap_planes = 0;        // planes the pad/grid buffers hold
     int64_t scratch_cap = 0;   // complex elements
@@ -725,6 +728,49 @@ int ensure_buffers(gbn_plan* P, int coils) {
     return ensure_scratch(P, coils);
 }
 
+// The last-axis pass runs on the plan's own pruned kernel (gbn_colfft.cu) in
+// single precision, 2-D and 3-D, for the lengths it implements, unless the
+// geometry asks for cuFFT throughout.  Its twiddles are computed here in
+// double precision and rounded once.
+int setup_colfft(gbn_plan* P) {
+    const gbn_geometry& G = P->geom;
+    const int L = G.Kd[G.ndim - 1];
+    P->colfft = !P->dbl && G.ndim >= 2 && !(G.flags & GBN_FLAG_CUFFT_ONLY) && colfft_supported(L);
+    if (!P->colfft) return GBN_OK;
+    std::vector<float> tw(2 * (size_t)L);
+    for (int m = 0; m < L; ++m) {
+        const double a = 6.283185307179586476925286766559 * (double)m / (double)L;   // 2 pi m / L
+        tw[2 * m] = (float)std::cos(a);
+        tw[2 * m + 1] = (float)-std::sin(a);
+    }
+    cudaError_t e = P->colfft_tw.alloc(tw.size() * sizeof(float));
+    if (e == cudaSuccess) e = cudaMemcpy(P->colfft_tw.p, tw.data(), tw.size() * sizeof(float), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return cuda_fail(e, "FFT twiddle table");
+    return GBN_OK;
+}
+
+// Last-axis pass over `planes` arrays of [K_last][S] at plane stride ps:
+// rows >= nin read as zero, rows >= nout not written.
+int run_colfft(gbn_plan* P, const void* in, int64_t in_elems, void* out, int64_t out_elems, int64_t S,
+               int64_t ps, int planes, int nin, int nout, int sign, cudaStream_t s) {
+    ColFftParams p;
+    std::memset(&p, 0, sizeof(p));
+    p.in = static_cast<const float2*>(in);
+    p.out = static_cast<float2*>(out);
+    p.S = S;
+    p.ps = ps;
+    p.planes = planes;
+    p.L = P->geom.Kd[P->geom.ndim - 1];
+    p.nin = nin;
+    p.nout = nout;
+    p.tw = static_cast<const float2*>(P->colfft_tw.p);
+    p.check = static_cast<unsigned*>(P->check.p);
+    p.in_elems = in_elems;
+    p.out_elems = out_elems;
+    GBN_CUDA(launch_colfft(p, sign, s), "last-axis FFT pass");
+    return GBN_OK;
+}
+
 int get_fft(gbn_plan* P, int planes, FftEntry** out) {
     for (auto& f : P->ffts)
         if (f.planes == planes) {
@@ -747,7 +793,7 @@ int get_fft(gbn_plan* P, int planes, FftEntry** out) {
         // every column along the last axis: stride batch_planes * slab, adjacent columns
         const int zs = batch_planes * slab;
         int ny[1] = {Kl}, emb[1] = {Kl};
-        r = cufftPlanMany(&f.hy, 1, ny, emb, zs, 1, emb, zs, 1, type, zs);
+        if (!P->colfft) r = cufftPlanMany(&f.hy, 1, ny, emb, zs, 1, emb, zs, 1, type, zs);
         if (r != CUFFT_SUCCESS) {
             cufftDestroy(f.hx);
             return cufft_fail(r, "cufftPlanMany (last axis)");
@@ -790,9 +836,20 @@ int fft_forward(gbn_plan* P, int planes, cudaStream_t s) {
         char* grid = static_cast<char*>(P->grid.p);
         for (int pl = 0; pl < planes; ++pl)
             if ((rc = exec_fft(P, f->hx, pad + pl * pb, mid + pl * pb, CUFFT_FORWARD, s))) return rc;
+        if (P->colfft)
+            return run_colfft(P, mid, (int64_t)P->mid_planes * P->Kprod, grid, (int64_t)P->cap_planes * P->Kprod,
+                              slab_cells(P), P->Kprod, planes, last_n(P), P->geom.Kd[2], -1, s);
         for (int pl = 0; pl < planes; ++pl)
             if ((rc = exec_fft(P, f->hy, mid + pl * pb, grid + pl * pb, CUFFT_FORWARD, s))) return rc;
         return GBN_OK;
+    }
+    if (P->geom.ndim == 2 && P->colfft) {
+        // the last-axis pass reads only the N_last * planes slabs the row
+        // pass writes
+        if ((rc = exec_fft(P, f->hx, P->pad.p, P->mid.p, CUFFT_FORWARD, s))) return rc;
+        const int64_t S = (int64_t)planes * P->geom.Kd[0];
+        return run_colfft(P, P->mid.p, (int64_t)P->mid_planes * P->Kprod, P->grid.p,
+                          (int64_t)P->cap_planes * P->Kprod, S, 0, 1, last_n(P), P->geom.Kd[1], -1, s);
     }
     if (P->geom.ndim == 2) {
         // The last-axis pass reads slabs [N_last * planes, K_last * planes)
@@ -826,14 +883,28 @@ int fft_inverse(gbn_plan* P, int planes, cudaStream_t s) {
     if (pruned_3d(P, planes)) {
         const size_t pb = (size_t)P->Kprod * 2 * P->rsize;
         char* grid = static_cast<char*>(P->grid.p);
-        for (int pl = 0; pl < planes; ++pl)
-            if ((rc = exec_fft(P, f->hy, grid + pl * pb, grid + pl * pb, CUFFT_INVERSE, s))) return rc;
+        if (P->colfft) {
+            const int64_t ge = (int64_t)P->cap_planes * P->Kprod;
+            if ((rc = run_colfft(P, grid, ge, grid, ge, slab_cells(P), P->Kprod, planes, P->geom.Kd[2], last_n(P),
+                                 1, s)))
+                return rc;
+        } else {
+            for (int pl = 0; pl < planes; ++pl)
+                if ((rc = exec_fft(P, f->hy, grid + pl * pb, grid + pl * pb, CUFFT_INVERSE, s))) return rc;
+        }
         for (int pl = 0; pl < planes; ++pl)
             if ((rc = exec_fft(P, f->hx, grid + pl * pb, grid + pl * pb, CUFFT_INVERSE, s))) return rc;
         return GBN_OK;
     }
     if (P->geom.ndim == 2) {
-        if ((rc = exec_fft(P, f->hy, P->grid.p, P->grid.p, CUFFT_INVERSE, s))) return rc;
+        if (P->colfft) {
+            const int64_t ge = (int64_t)P->cap_planes * P->Kprod;
+            if ((rc = run_colfft(P, P->grid.p, ge, P->grid.p, ge, (int64_t)planes * P->geom.Kd[0], 0, 1,
+                                 P->geom.Kd[1], last_n(P), 1, s)))
+                return rc;
+        } else if ((rc = exec_fft(P, f->hy, P->grid.p, P->grid.p, CUFFT_INVERSE, s))) {
+            return rc;
+        }
         return exec_fft(P, f->hx, P->grid.p, P->grid.p, CUFFT_INVERSE, s);
     }
     return exec_fft(P, f->h, P->grid.p, P->grid.p, CUFFT_INVERSE, s);
@@ -1636,6 +1707,10 @@ int gbn_plan_create(gbn_plan** out, const gbn_geometry* geom, const void* const*
         P->Nprod *= geom->Nd[d];
     }
     choose_tiles(P);
+    if ((rc = setup_colfft(P))) {
+        delete P;
+        return rc;
+    }
     {
         cudaError_t e = P->check.alloc(16);
         if (e == cudaSuccess) e = cudaMemset(P->check.p, 0, 16);
