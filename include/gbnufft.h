@@ -57,7 +57,7 @@ extern "C" {
 #define GBN_FLAG_TABLE_ONLY 1
 /* By default the single-precision 2-D and 3-D plans run the FFT's pass
  * along the slowest axis on the library's own pruned kernel when that
- * axis's length is 64, 96, 128, 192, 256, 384, 512, 768 or 1024 (it reads
+ * axis's length is 64, 96, 128, 192, 256, 384, 512 or 768 (it reads
  * only the rows that hold data and writes only the rows the crop reads);
  * CUFFT_ONLY runs every pass through cuFFT instead.                         */
 #define GBN_FLAG_CUFFT_ONLY 2

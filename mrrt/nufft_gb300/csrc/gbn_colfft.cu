@@ -71,7 +71,29 @@ __constant__ float2 c_root96[96] = {GBN_ROOT16(0), GBN_ROOT16(16), GBN_ROOT16(32
 #undef GBN_ROOT4
 #undef GBN_ROOT
 
-__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+// Complex add and subtract as one packed f32x2 instruction each (the
+// butterflies' adds are most of their work: 2-D 512-point pass 61 -> 57 us,
+// 3-D 256-point 661 -> 554 us with the split below).
+__device__ __forceinline__ unsigned long long pack2(float2 a) {
+    unsigned long long r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a.x), "f"(a.y));
+    return r;
+}
+__device__ __forceinline__ float2 unpack2(unsigned long long r) {
+    float2 d;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(d.x), "=f"(d.y) : "l"(r));
+    return d;
+}
+__device__ __forceinline__ float2 padd(float2 a, float2 b) {
+    unsigned long long r;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(pack2(a)), "l"(pack2(b)));
+    return unpack2(r);
+}
+__device__ __forceinline__ float2 psub(float2 a, float2 b) {
+    unsigned long long r;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(pack2(a)), "l"(pack2(b)));
+    return unpack2(r);
+}
 // multiply by i^(SIGN), i.e. -i forward, +i inverse
 template <int SIGN>
 __device__ __forceinline__ float2 mul_si(float2 a) { return SIGN < 0 ? make_float2(a.y, -a.x) : make_float2(-a.y, a.x); }
@@ -93,26 +115,26 @@ template <int R, int SIGN>
 __device__ __forceinline__ void butterfly(float2 (&v)[R]) {
     if constexpr (R == 2) {
         const float2 a = v[0];
-        v[0] = cadd(a, v[1]);
-        v[1] = csub(a, v[1]);
+        v[0] = padd(a, v[1]);
+        v[1] = psub(a, v[1]);
     } else if constexpr (R == 4) {
-        const float2 t0 = cadd(v[0], v[2]), t1 = csub(v[0], v[2]);
-        const float2 t2 = cadd(v[1], v[3]), t3 = mul_si<SIGN>(csub(v[1], v[3]));
-        v[0] = cadd(t0, t2);
-        v[2] = csub(t0, t2);
-        v[1] = cadd(t1, t3);
-        v[3] = csub(t1, t3);
+        const float2 t0 = padd(v[0], v[2]), t1 = psub(v[0], v[2]);
+        const float2 t2 = padd(v[1], v[3]), t3 = mul_si<SIGN>(psub(v[1], v[3]));
+        v[0] = padd(t0, t2);
+        v[2] = psub(t0, t2);
+        v[1] = padd(t1, t3);
+        v[3] = psub(t1, t3);
     } else {
         static_assert(R == 3, "radix 2, 3 or 4");
         // w = exp(SIGN 2 pi i / 3) = -1/2 + SIGN i sqrt(3)/2
         constexpr float h = 0.866025403784438646763723f;   // sqrt(3) / 2
-        const float2 t = cadd(v[1], v[2]);
-        const float2 d = csub(v[1], v[2]);
+        const float2 t = padd(v[1], v[2]);
+        const float2 d = psub(v[1], v[2]);
         const float2 u = SIGN < 0 ? make_float2(h * d.y, -h * d.x) : make_float2(-h * d.y, h * d.x);
         const float2 m = make_float2(v[0].x - 0.5f * t.x, v[0].y - 0.5f * t.y);
-        v[0] = cadd(v[0], t);
-        v[1] = cadd(m, u);
-        v[2] = csub(m, u);
+        v[0] = padd(v[0], t);
+        v[1] = padd(m, u);
+        v[2] = psub(m, u);
     }
 }
 
@@ -212,10 +234,11 @@ cudaError_t colfft_launch(const ColFftParams& p, int sign, cudaStream_t s) {
 
 }  // namespace
 
-// Lengths with a compile-time split L1 x L2 (both dividing 96, at most 32).
+// Lengths with a compile-time split L1 x L2 (both dividing 96, at most 32)
+// that measured faster than cuFFT.
 bool colfft_supported(int L) {
     switch (L) {
-        case 64: case 96: case 128: case 192: case 256: case 384: case 512: case 768: case 1024:
+        case 64: case 96: case 128: case 192: case 256: case 384: case 512: case 768:
             return true;
         default:
             return false;
@@ -225,22 +248,26 @@ bool colfft_supported(int L) {
 cudaError_t launch_colfft(const ColFftParams& p, int sign, cudaStream_t s) {
     if (p.S <= 0 || p.planes <= 0 || p.nin < 0 || p.nin > p.L || p.nout < 0 || p.nout > p.L)
         return cudaErrorInvalidValue;
-    // Splits measured on a GB300 (forward + inverse, L2 larger than the data):
-    //   512, 16384 columns: 32 x 16 with 8 columns per CTA 63 us, 16 x 32
-    //     with 16 columns 70 us, cuFFT 64 us;
-    //   384, 196608 columns: 16 x 24 363 us, 24 x 16 367 us, cuFFT 732 us;
-    //   256, 8 planes of 65536 columns: 16 x 16 679 us, 8 x 32 696 us,
-    //     cuFFT 809 us.
+    // Splits measured on a GB300 (forward + inverse, packed butterflies):
+    //   512, 16384 columns: 16 x 32 with 16 columns per CTA 57 us, 32 x 16
+    //     with 8 columns 58 us, cuFFT 62 us;
+    //   384, 196608 columns: 16 x 24 321 us, 24 x 16 337 us, cuFFT 694 us;
+    //   256, 8 planes of 65536 columns: 8 x 32 554 us, 16 x 16 662 us,
+    //     cuFFT 808 us;
+    //   128, 4 planes of 32768 columns: 8 x 16 73 us, 16 x 8 81 us, cuFFT 134 us;
+    //   192: 16 x 12 116 us, 8 x 24 120 us, cuFFT 214 us; 768: 32 x 24 109 us,
+    //     24 x 32 128 us, cuFFT 255 us.
+    // 1024 (32 x 32, one CTA per SM at 242 registers) ran slower than cuFFT
+    // (152 against about 139 us at 16384 columns) and is left to cuFFT.
     switch (p.L) {
         case 64: return colfft_launch<8, 8>(p, sign, s);
         case 96: return colfft_launch<8, 12>(p, sign, s);
-        case 128: return colfft_launch<16, 8>(p, sign, s);
+        case 128: return colfft_launch<8, 16>(p, sign, s);
         case 192: return colfft_launch<16, 12>(p, sign, s);
-        case 256: return colfft_launch<16, 16>(p, sign, s);
+        case 256: return colfft_launch<8, 32>(p, sign, s);
         case 384: return colfft_launch<16, 24>(p, sign, s);
-        case 512: return colfft_launch<32, 16>(p, sign, s);
+        case 512: return colfft_launch<16, 32, 16>(p, sign, s);
         case 768: return colfft_launch<32, 24>(p, sign, s);
-        case 1024: return colfft_launch<32, 32>(p, sign, s);
         default: return cudaErrorInvalidValue;
     }
 }
