@@ -297,6 +297,25 @@ bool colfft_supported(int L);
 // sign -1: forward (exp(-2 pi i nk / L)), +1: inverse (unnormalised)
 cudaError_t launch_colfft(const ColFftParams& p, int sign, cudaStream_t s);
 
+// Row passes of the 2-D transform with pad / crop folded in (gbn_rowfft.cu).
+// Rows r < planes * N1: plane r / N1, row r % N1 of the image
+// [planes][N1][N0] and of the grid (slab at plane * gsp + row * gs1, L = K0
+// values).  sign -1: sn * image -> forward FFT -> grid slab; +1: grid slab ->
+// inverse FFT -> first N0 values * scale * sn -> image.
+struct RowFftParams {
+    const float2* in;               // forward: image; inverse: grid
+    float2* out;                    // forward: grid; inverse: image
+    const float* sn;                // [N1][N0]
+    float scale;                    // inverse only
+    int planes, N0, N1, L;
+    int64_t gsp, gs1;
+    const float2* tw;               // exp(-2 pi i m / L), m < L
+    unsigned* check;                // checked builds: status word and extents
+    int64_t in_elems, out_elems;
+};
+bool rowfft_supported(int L);
+cudaError_t launch_rowfft(const RowFftParams& p, int sign, cudaStream_t s);
+
 template <typename R> cudaError_t launch_gather(const GatherParams<R>& p, cudaStream_t s);
 template <typename R> cudaError_t launch_spread(const SpreadParams<R>& p, cudaStream_t s);
 template <typename R> cudaError_t launch_reduce(const ReduceParams<R>& p, cudaStream_t s);

@@ -221,6 +221,8 @@ struct gbn_plan {
     int64_t mid_clean = 0;     // 2-D: slabs from which mid is known to be zero
     bool colfft = false;       // last-axis pass by gbn_colfft.cu (else cuFFT)
     DevBuf colfft_tw;          // its twiddles exp(-2 pi i m / K_last), m < K_last
+    bool rowfft = false;       // 2-D: row passes with pad / crop folded in (gbn_rowfft.cu)
+    DevBuf rowfft_tw;          // their twiddles, m < K_0
     int mid_planes = 0;        // planes the mid buffer holds
     int cap_planes = 0;        // planes the pad/grid buffers hold
     int64_t scratch_cap = 0;   // complex elements
@@ -732,20 +734,56 @@ int ensure_buffers(gbn_plan* P, int coils) {
 // single precision, 2-D and 3-D, for the lengths it implements, unless the
 // geometry asks for cuFFT throughout.  Its twiddles are computed here in
 // double precision and rounded once.
-int setup_colfft(gbn_plan* P) {
-    const gbn_geometry& G = P->geom;
-    const int L = G.Kd[G.ndim - 1];
-    P->colfft = !P->dbl && G.ndim >= 2 && !(G.flags & GBN_FLAG_CUFFT_ONLY) && colfft_supported(L);
-    if (!P->colfft) return GBN_OK;
+int upload_twiddles(DevBuf& dst, int L) {
     std::vector<float> tw(2 * (size_t)L);
     for (int m = 0; m < L; ++m) {
         const double a = 6.283185307179586476925286766559 * (double)m / (double)L;   // 2 pi m / L
         tw[2 * m] = (float)std::cos(a);
         tw[2 * m + 1] = (float)-std::sin(a);
     }
-    cudaError_t e = P->colfft_tw.alloc(tw.size() * sizeof(float));
-    if (e == cudaSuccess) e = cudaMemcpy(P->colfft_tw.p, tw.data(), tw.size() * sizeof(float), cudaMemcpyHostToDevice);
+    cudaError_t e = dst.alloc(tw.size() * sizeof(float));
+    if (e == cudaSuccess) e = cudaMemcpy(dst.p, tw.data(), tw.size() * sizeof(float), cudaMemcpyHostToDevice);
     if (e != cudaSuccess) return cuda_fail(e, "FFT twiddle table");
+    return GBN_OK;
+}
+
+// In 2-D the row passes also run on the plan's own kernels, with the pad and
+// the crop folded in (gbn_rowfft.cu), when the last-axis pass does and K_0
+// has a supported length.
+int setup_colfft(gbn_plan* P) {
+    const gbn_geometry& G = P->geom;
+    const int L = G.Kd[G.ndim - 1];
+    P->colfft = !P->dbl && G.ndim >= 2 && !(G.flags & GBN_FLAG_CUFFT_ONLY) && colfft_supported(L);
+    if (!P->colfft) return GBN_OK;
+    int rc = upload_twiddles(P->colfft_tw, L);
+    if (rc) return rc;
+    P->rowfft = G.ndim == 2 && rowfft_supported(G.Kd[0]);
+    if (P->rowfft) rc = upload_twiddles(P->rowfft_tw, G.Kd[0]);
+    return rc;
+}
+
+// 2-D row pass with the pad (sign -1: image -> mid) or the crop (sign +1:
+// grid -> image) folded in.
+int run_rowfft(gbn_plan* P, const void* in, int64_t in_elems, void* out, int64_t out_elems, int planes, int sign,
+               cudaStream_t s) {
+    const gbn_geometry& G = P->geom;
+    RowFftParams p;
+    std::memset(&p, 0, sizeof(p));
+    p.in = static_cast<const float2*>(in);
+    p.out = static_cast<float2*>(out);
+    p.sn = static_cast<const float*>(P->sn.p);
+    p.scale = G.ortho ? (float)(G.adjoint_scale / std::sqrt((double)P->Kprod)) : (float)G.adjoint_scale;
+    p.planes = planes;
+    p.N0 = G.Nd[0];
+    p.N1 = G.Nd[1];
+    p.L = G.Kd[0];
+    p.gsp = G.Kd[0];
+    p.gs1 = (int64_t)planes * G.Kd[0];
+    p.tw = static_cast<const float2*>(P->rowfft_tw.p);
+    p.check = static_cast<unsigned*>(P->check.p);
+    p.in_elems = in_elems;
+    p.out_elems = out_elems;
+    GBN_CUDA(launch_rowfft(p, sign, s), sign < 0 ? "pad + row FFT pass" : "row FFT pass + crop");
     return GBN_OK;
 }
 
@@ -820,6 +858,17 @@ int exec_fft(gbn_plan* P, cufftHandle h, void* in, void* out, int dir, cudaStrea
     return GBN_OK;
 }
 
+// 2-D last-axis pass: forward mid -> grid (the N_1 slabs with data read),
+// inverse grid -> grid in place (the N_1 slabs the crop reads written).
+int colfft_2d(gbn_plan* P, int planes, int sign, cudaStream_t s) {
+    const int64_t S = (int64_t)planes * P->geom.Kd[0];
+    const int64_t ge = (int64_t)P->cap_planes * P->Kprod;
+    if (sign < 0)
+        return run_colfft(P, P->mid.p, (int64_t)P->mid_planes * P->Kprod, P->grid.p, ge, S, 0, 1, last_n(P),
+                          P->geom.Kd[1], -1, s);
+    return run_colfft(P, P->grid.p, ge, P->grid.p, ge, S, 0, 1, P->geom.Kd[1], last_n(P), 1, s);
+}
+
 // Forward Kd-point FFT of the padded planes into the grid.  2-D and 3-D:
 // the slab pass only over the N_last slabs that hold data (pad -> mid), then
 // the last-axis pass over every column (mid -> grid).
@@ -847,9 +896,7 @@ int fft_forward(gbn_plan* P, int planes, cudaStream_t s) {
         // the last-axis pass reads only the N_last * planes slabs the row
         // pass writes
         if ((rc = exec_fft(P, f->hx, P->pad.p, P->mid.p, CUFFT_FORWARD, s))) return rc;
-        const int64_t S = (int64_t)planes * P->geom.Kd[0];
-        return run_colfft(P, P->mid.p, (int64_t)P->mid_planes * P->Kprod, P->grid.p,
-                          (int64_t)P->cap_planes * P->Kprod, S, 0, 1, last_n(P), P->geom.Kd[1], -1, s);
+        return colfft_2d(P, planes, -1, s);
     }
     if (P->geom.ndim == 2) {
         // The last-axis pass reads slabs [N_last * planes, K_last * planes)
@@ -898,10 +945,7 @@ int fft_inverse(gbn_plan* P, int planes, cudaStream_t s) {
     }
     if (P->geom.ndim == 2) {
         if (P->colfft) {
-            const int64_t ge = (int64_t)P->cap_planes * P->Kprod;
-            if ((rc = run_colfft(P, P->grid.p, ge, P->grid.p, ge, (int64_t)planes * P->geom.Kd[0], 0, 1,
-                                 P->geom.Kd[1], last_n(P), 1, s)))
-                return rc;
+            if ((rc = colfft_2d(P, planes, 1, s))) return rc;
         } else if ((rc = exec_fft(P, f->hy, P->grid.p, P->grid.p, CUFFT_INVERSE, s))) {
             return rc;
         }
@@ -1082,6 +1126,18 @@ int run_forward(gbn_plan* P, const void* x, void* y, int coils, cudaStream_t s, 
     pp.x_elems = (int64_t)(maps ? P->F : P->F * coils) * P->Nprod;
     pp.out_elems = (int64_t)P->cap_planes * P->Kprod;
     internal_layout(P, P->F * coils, pp);
+    if (P->rowfft && !maps) {
+        // single precision only (rowfft is off for double plans)
+        {
+            NvtxRange r("gbn forward: pad + fft");
+            if ((rc = run_rowfft(P, x, pp.x_elems, P->mid.p, (int64_t)P->mid_planes * P->Kprod, P->F * coils, -1,
+                                 s)))
+                return rc;
+            if ((rc = colfft_2d(P, P->F * coils, -1, s))) return rc;
+        }
+        NvtxRange r("gbn forward: gather");
+        return run_gather<R>(P, P->grid.p, y, coils, true, s);
+    }
     {
         NvtxRange r("gbn forward: pad");
         GBN_CUDA(launch_pad<R>(pp, s), "pad launch");
@@ -1105,6 +1161,12 @@ int run_adjoint(gbn_plan* P, const void* y, void* x, int coils, cudaStream_t s, 
         NvtxRange r("gbn adjoint: spread");
         rc = run_spread<R>(P, y, P->grid.p, coils, true, s);
         if (rc) return rc;
+    }
+    if (P->rowfft && !maps) {
+        NvtxRange r("gbn adjoint: fft + crop");
+        if ((rc = colfft_2d(P, P->F * coils, 1, s))) return rc;
+        return run_rowfft(P, P->grid.p, (int64_t)P->cap_planes * P->Kprod, x, (int64_t)P->F * coils * P->Nprod,
+                          P->F * coils, 1, s);
     }
     {
         NvtxRange r("gbn adjoint: fft");

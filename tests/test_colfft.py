@@ -1,8 +1,10 @@
-"""The plan's own pruned last-axis FFT pass (gbn_colfft.cu) against cuFFT.
+"""The plan's own FFT passes (gbn_colfft.cu, gbn_rowfft.cu) against cuFFT.
 
 Single-precision 2-D and 3-D plans run the FFT's pass along the slowest axis
-on the library's kernel when that axis has a supported length; a plan made
-with cufft_only (GBN_FLAG_CUFFT_ONLY) runs every pass through cuFFT.  Both
+on the library's kernel when that axis has a supported length, and 2-D plans
+with a supported K0 also the row passes with the pad and crop folded in; a
+plan made with cufft_only (GBN_FLAG_CUFFT_ONLY) runs every pass through cuFFT
+around the separate pad and crop kernels.  Both
 compute the same transform in float32 by different factorisations, so the
 forward and adjoint NUFFTs agree to float32 rounding (relative L2 2e-6; the
 measured differences are near 2e-7).  The cases cover every supported length,
@@ -21,7 +23,7 @@ pytestmark = pytest.mark.gpu
 TOL = 2e-6
 
 
-def _pair(N, K, J, coils=2, frames=1, M=1500, seed=0, rdt=np.float32):
+def _pair(N, K, J, coils=2, frames=1, M=1500, seed=0, rdt=np.float32, **kw):
     from mrrt.nufft_gb300._kernels import kernel_table
     from mrrt.nufft_gb300._plan import GpuPlan
 
@@ -32,7 +34,7 @@ def _pair(N, K, J, coils=2, frames=1, M=1500, seed=0, rdt=np.float32):
     sn = rng.uniform(0.5, 1.5, int(np.prod(N))).astype(rdt)
     foff = np.arange(frames + 1, dtype=np.int64) * M
     return [GpuPlan(N, K, J, 256, rdt, h, None, sn, tm, None, frame_offsets=foff, max_coils=coils,
-                    cufft_only=flag) for flag in (False, True)]
+                    cufft_only=flag, **kw) for flag in (False, True)]
 
 
 def _run(plans, coils, frames, seed=1):
@@ -94,5 +96,27 @@ def test_headline_geometry_against_cufft(gpu_lib):
     N, K, J, coils = (256, 256), (512, 512), (6, 6), 32
     plans = _pair(N, K, J, coils=coils, M=4000)
     ys, xs = _run(plans, coils, 1)
+    assert rel_l2(ys[0], ys[1]) < TOL
+    assert rel_l2(xs[0], xs[1]) < TOL
+
+
+@pytest.mark.parametrize("K0", [64, 96, 128, 192, 256, 384, 512, 768])
+def test_2d_fused_row_passes(gpu_lib, K0):
+    """A supported K0 runs the row passes with the pad and the crop folded in
+    (gbn_rowfft.cu): image rows of N0 = K0/2 - 1 values, 30 of 64 rows, two
+    frames of three coils."""
+    N, K, J = (K0 // 2 - 1, 30), (K0, 64), (6, 6)
+    plans = _pair(N, K, J, coils=3, frames=2, seed=K0)
+    ys, xs = _run(plans, 3, 2)
+    assert rel_l2(ys[0], ys[1]) < TOL
+    assert rel_l2(xs[0], xs[1]) < TOL
+
+
+def test_2d_fused_row_passes_orthonormal_scaling(gpu_lib):
+    """The crop's scale (orthonormal FFT, adjoint_scale) is applied by the
+    fused pass."""
+    N, K, J = (64, 64), (128, 128), (6, 6)
+    plans = _pair(N, K, J, coils=2, ortho=True, adjoint_scale=1.7)
+    ys, xs = _run(plans, 2, 1)
     assert rel_l2(ys[0], ys[1]) < TOL
     assert rel_l2(xs[0], xs[1]) < TOL
