@@ -1,11 +1,12 @@
-// Pruned FFT pass along the slowest axis of the oversampled grid.
+// Pruned FFT pass along a strided axis of the oversampled grid.
 //
 // The oversampled FFT (mrrt/nufft/_nufft.py:1330-1350 forward fftn of the
 // zero-padded image, :1561-1572 adjoint ifftn before the crop) is done in
-// passes.  Its last pass runs along the slowest memory axis (axis 1 in 2-D,
-// axis 2 in 3-D): an [L][S] array -- S columns, row stride S -- transformed
-// along L for every column, for one or several planes at a plane stride.
-// Half of that axis is zero padding:
+// passes.  Every pass but the first runs along a strided memory axis (axis 1
+// in 2-D; axes 1 and 2 in 3-D): an [L][S] array -- S columns, row stride S
+// -- transformed along L for every column, for a set of such arrays at two
+// strides (planes; z-slabs within a plane).  Half of that axis is zero
+// padding:
 //   * forward, only the first nin = N_last rows hold data; rows past nin are
 //     zero and are not read;
 //   * inverse, only the first nout = N_last rows are used afterwards (the
@@ -38,12 +39,16 @@ namespace gbn {
 
 namespace {
 
-template <int L1, int L2, int CF_TC, int SIGN>
+// Z: the arrays have a second stride (blockIdx.z; the 3-D axis-1 pass).  A
+// separate instantiation: with the second term in every kernel the 2-D
+// 512-point pass compiled to 86 instead of 80 registers, two 256-thread CTAs
+// per SM instead of three, and ran 40% slower.
+template <int L1, int L2, int CF_TC, int SIGN, bool Z>
 __global__ void __launch_bounds__(CF_TC * L1) colfft_kernel(const ColFftParams p) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float2* sm = reinterpret_cast<float2*>(smem_raw);
     const int64_t c0 = (int64_t)blockIdx.x * CF_TC;
-    const int64_t pb = (int64_t)blockIdx.y * p.ps;
+    const int64_t pb = (int64_t)blockIdx.y * p.ps + (Z ? (int64_t)blockIdx.z * p.ps2 : 0);
 
     // step A: (column, n1), L2-point transforms of rows n1 + L1 n2
     {
@@ -91,17 +96,24 @@ template <int L1, int L2, int CF_TC>
 cudaError_t colfft_launch(const ColFftParams& p, int sign, cudaStream_t s) {
     constexpr int L = L1 * L2;
     const size_t smem = (size_t)CF_TC * L * sizeof(float2);
-    const void* k = sign < 0 ? reinterpret_cast<const void*>(colfft_kernel<L1, L2, CF_TC, -1>)
-                             : reinterpret_cast<const void*>(colfft_kernel<L1, L2, CF_TC, 1>);
+    const bool z = p.planes2 > 1;
+    const void* k = sign < 0 ? (z ? reinterpret_cast<const void*>(colfft_kernel<L1, L2, CF_TC, -1, true>)
+                                  : reinterpret_cast<const void*>(colfft_kernel<L1, L2, CF_TC, -1, false>))
+                             : (z ? reinterpret_cast<const void*>(colfft_kernel<L1, L2, CF_TC, 1, true>)
+                                  : reinterpret_cast<const void*>(colfft_kernel<L1, L2, CF_TC, 1, false>));
     cudaError_t e = ensure_dynamic_smem(k, smem);
     if (e != cudaSuccess) return e;
     const int64_t ctas = (p.S + CF_TC - 1) / CF_TC;
-    if (ctas > INT32_MAX || p.planes > 65535) return cudaErrorInvalidValue;
-    const dim3 grid((unsigned)ctas, (unsigned)p.planes);
-    if (sign < 0)
-        colfft_kernel<L1, L2, CF_TC, -1><<<grid, CF_TC * L1, smem, s>>>(p);
+    if (ctas > INT32_MAX || p.planes > 65535 || p.planes2 > 65535) return cudaErrorInvalidValue;
+    const dim3 grid((unsigned)ctas, (unsigned)p.planes, (unsigned)p.planes2);
+    if (sign < 0 && z)
+        colfft_kernel<L1, L2, CF_TC, -1, true><<<grid, CF_TC * L1, smem, s>>>(p);
+    else if (sign < 0)
+        colfft_kernel<L1, L2, CF_TC, -1, false><<<grid, CF_TC * L1, smem, s>>>(p);
+    else if (z)
+        colfft_kernel<L1, L2, CF_TC, 1, true><<<grid, CF_TC * L1, smem, s>>>(p);
     else
-        colfft_kernel<L1, L2, CF_TC, 1><<<grid, CF_TC * L1, smem, s>>>(p);
+        colfft_kernel<L1, L2, CF_TC, 1, false><<<grid, CF_TC * L1, smem, s>>>(p);
     return cudaGetLastError();
 }
 
@@ -119,7 +131,7 @@ bool colfft_supported(int L) {
 }
 
 cudaError_t launch_colfft(const ColFftParams& p, int sign, cudaStream_t s) {
-    if (p.S <= 0 || p.planes <= 0 || p.nin < 0 || p.nin > p.L || p.nout < 0 || p.nout > p.L)
+    if (p.S <= 0 || p.planes <= 0 || p.planes2 <= 0 || p.nin < 0 || p.nin > p.L || p.nout < 0 || p.nout > p.L)
         return cudaErrorInvalidValue;
     // Splits measured on a GB300 (forward + inverse, packed butterflies):
     //   512, 16384 columns: 16 x 32 with 16 columns per CTA 57 us, 32 x 16

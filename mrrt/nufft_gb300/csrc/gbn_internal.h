@@ -279,15 +279,16 @@ cudaError_t launch_permute_int4(const int4* in, const unsigned* order, int64_t n
 cudaError_t launch_permute_int2(const int2* in, const unsigned* order, int64_t n, int2* out, cudaStream_t s);
 template <typename R> cudaError_t launch_bin_pack(const PackParams<R>& p, cudaStream_t s);
 
-// Pruned FFT pass along the slowest axis (gbn_colfft.cu): `planes` arrays
-// at plane stride ps, each [L][S] (S columns, row stride S); rows >= nin
-// are read as zero, rows >= nout are not written.  in == out is allowed.
+// Pruned FFT pass along a strided axis (gbn_colfft.cu): planes x planes2
+// arrays at offsets y * ps + z * ps2, each [L][S] (S columns, row stride S);
+// rows >= nin are read as zero, rows >= nout are not written.  in == out is
+// allowed.
 struct ColFftParams {
     const float2* in;
     float2* out;
-    int64_t S;                      // columns per plane, and the row stride (elements)
-    int64_t ps;                     // plane stride (elements)
-    int planes;
+    int64_t S;                      // columns per array, and the row stride (elements)
+    int64_t ps, ps2;                // array strides (elements)
+    int planes, planes2;
     int L, nin, nout;
     const float2* tw;               // exp(-2 pi i m / L), m < L
     unsigned* check;                // checked builds: status word and extents
@@ -297,18 +298,19 @@ bool colfft_supported(int L);
 // sign -1: forward (exp(-2 pi i nk / L)), +1: inverse (unnormalised)
 cudaError_t launch_colfft(const ColFftParams& p, int sign, cudaStream_t s);
 
-// Row passes of the 2-D transform with pad / crop folded in (gbn_rowfft.cu).
-// Rows r < planes * N1: plane r / N1, row r % N1 of the image
-// [planes][N1][N0] and of the grid (slab at plane * gsp + row * gs1, L = K0
-// values).  sign -1: sn * image -> forward FFT -> grid slab; +1: grid slab ->
-// inverse FFT -> first N0 values * scale * sn -> image.
+// Row passes of the 2-D and 3-D transforms with pad / crop folded in
+// (gbn_rowfft.cu).  Rows r < planes * N2 * N1 (N2 = 1 in 2-D): plane
+// r / (N1 N2), image row (n2, n1) of [planes][N2][N1][N0] and grid row at
+// plane * gsp + n2 * gs2 + n1 * gs1 (L = K0 values).  sign -1: sn * image ->
+// forward FFT -> grid row; +1: grid row -> inverse FFT -> first N0 values *
+// scale * sn -> image.
 struct RowFftParams {
     const float2* in;               // forward: image; inverse: grid
     float2* out;                    // forward: grid; inverse: image
-    const float* sn;                // [N1][N0]
+    const float* sn;                // [N2][N1][N0]
     float scale;                    // inverse only
-    int planes, N0, N1, L;
-    int64_t gsp, gs1;
+    int planes, N0, N1, N2, L;
+    int64_t gsp, gs1, gs2;
     const float2* tw;               // exp(-2 pi i m / L), m < L
     unsigned* check;                // checked builds: status word and extents
     int64_t in_elems, out_elems;

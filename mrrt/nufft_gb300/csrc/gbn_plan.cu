@@ -220,9 +220,9 @@ struct gbn_plan {
                           // slabs >= N_last the last-axis pass reads stay zero
     int64_t mid_clean = 0;     // 2-D: slabs from which mid is known to be zero
     bool colfft = false;       // last-axis pass by gbn_colfft.cu (else cuFFT)
-    DevBuf colfft_tw;          // its twiddles exp(-2 pi i m / K_last), m < K_last
-    bool rowfft = false;       // 2-D: row passes with pad / crop folded in (gbn_rowfft.cu)
-    DevBuf rowfft_tw;          // their twiddles, m < K_0
+    bool rowfft = false;       // every pass on the plan's kernels, the row passes with the pad
+                               // and crop folded in (gbn_rowfft.cu, gbn_colfft.cu)
+    DevBuf fft_tw[3];          // per axis d: exp(-2 pi i m / K_d), m < K_d (axes those use)
     int mid_planes = 0;        // planes the mid buffer holds
     int cap_planes = 0;        // planes the pad/grid buffers hold
     int64_t scratch_cap = 0;   // complex elements
@@ -702,7 +702,9 @@ int ensure_scratch(gbn_plan* P, int coils) {
 }
 
 // Zero-padded FFT input, FFT output grid and scratch for F * coils planes.
-int ensure_buffers(gbn_plan* P, int coils) {
+// `fused`: the call runs the 3-D transform on the plan's own passes (in
+// place on the grid), which need no slab-pass buffer.
+int ensure_buffers(gbn_plan* P, int coils, bool fused = false) {
     const int planes = P->F * coils;
     const size_t csz = (size_t)2 * P->rsize;
     if (planes > P->cap_planes) {
@@ -717,7 +719,7 @@ int ensure_buffers(gbn_plan* P, int coils) {
     }
     // the pruned FFT's intermediate buffer: every plane in 2-D, the planes of
     // a pruned call in 3-D (none beyond PRUNE3_MAX_PLANES)
-    const int mid_need = P->geom.ndim == 2 || pruned_3d(P, planes) ? planes : 0;
+    const int mid_need = P->geom.ndim == 2 || (pruned_3d(P, planes) && !fused) ? planes : 0;
     if (mid_need > P->mid_planes) {
         const size_t bytes = (size_t)mid_need * P->Kprod * csz;
         cudaError_t e = P->mid.alloc(bytes);
@@ -747,23 +749,26 @@ int upload_twiddles(DevBuf& dst, int L) {
     return GBN_OK;
 }
 
-// In 2-D the row passes also run on the plan's own kernels, with the pad and
-// the crop folded in (gbn_rowfft.cu), when the last-axis pass does and K_0
-// has a supported length.
+// When every axis has a supported length, the whole transform runs on the
+// plan's kernels, the row passes with the pad and the crop folded in
+// (gbn_rowfft.cu).
 int setup_colfft(gbn_plan* P) {
     const gbn_geometry& G = P->geom;
     const int L = G.Kd[G.ndim - 1];
     P->colfft = !P->dbl && G.ndim >= 2 && !(G.flags & GBN_FLAG_CUFFT_ONLY) && colfft_supported(L);
     if (!P->colfft) return GBN_OK;
-    int rc = upload_twiddles(P->colfft_tw, L);
-    if (rc) return rc;
-    P->rowfft = G.ndim == 2 && rowfft_supported(G.Kd[0]);
-    if (P->rowfft) rc = upload_twiddles(P->rowfft_tw, G.Kd[0]);
-    return rc;
+    P->rowfft = rowfft_supported(G.Kd[0]) && (G.ndim == 2 || colfft_supported(G.Kd[1]));
+    for (int d = 0; d < G.ndim; ++d) {
+        if (d < G.ndim - 1 && !P->rowfft) continue;
+        int rc = upload_twiddles(P->fft_tw[d], G.Kd[d]);
+        if (rc) return rc;
+    }
+    return GBN_OK;
 }
 
-// 2-D row pass with the pad (sign -1: image -> mid) or the crop (sign +1:
-// grid -> image) folded in.
+// Row pass with the pad (sign -1: image -> grid rows) or the crop (sign +1:
+// grid rows -> image) folded in; 2-D: image rows to the row-interleaved
+// layout (into mid), 3-D: to the plane-major layout (the grid in place).
 int run_rowfft(gbn_plan* P, const void* in, int64_t in_elems, void* out, int64_t out_elems, int planes, int sign,
                cudaStream_t s) {
     const gbn_geometry& G = P->geom;
@@ -776,10 +781,10 @@ int run_rowfft(gbn_plan* P, const void* in, int64_t in_elems, void* out, int64_t
     p.planes = planes;
     p.N0 = G.Nd[0];
     p.N1 = G.Nd[1];
+    p.N2 = G.ndim > 2 ? G.Nd[2] : 1;
     p.L = G.Kd[0];
-    p.gsp = G.Kd[0];
-    p.gs1 = (int64_t)planes * G.Kd[0];
-    p.tw = static_cast<const float2*>(P->rowfft_tw.p);
+    internal_layout(P, planes, p);
+    p.tw = static_cast<const float2*>(P->fft_tw[0].p);
     p.check = static_cast<unsigned*>(P->check.p);
     p.in_elems = in_elems;
     p.out_elems = out_elems;
@@ -787,25 +792,37 @@ int run_rowfft(gbn_plan* P, const void* in, int64_t in_elems, void* out, int64_t
     return GBN_OK;
 }
 
-// Last-axis pass over `planes` arrays of [K_last][S] at plane stride ps:
-// rows >= nin read as zero, rows >= nout not written.
-int run_colfft(gbn_plan* P, const void* in, int64_t in_elems, void* out, int64_t out_elems, int64_t S,
-               int64_t ps, int planes, int nin, int nout, int sign, cudaStream_t s) {
+// Pass along memory axis `axis` (1 or 2) over planes x planes2 arrays of
+// [K_axis][S] at strides ps, ps2: rows >= nin read as zero, rows >= nout not
+// written.
+struct AxisPass {
+    const void* in;
+    int64_t in_elems;
+    void* out;
+    int64_t out_elems;
+    int axis;
+    int64_t S, ps, ps2;
+    int planes, planes2;
+    int nin, nout;
+};
+int run_colfft(gbn_plan* P, const AxisPass& a, int sign, cudaStream_t s) {
     ColFftParams p;
     std::memset(&p, 0, sizeof(p));
-    p.in = static_cast<const float2*>(in);
-    p.out = static_cast<float2*>(out);
-    p.S = S;
-    p.ps = ps;
-    p.planes = planes;
-    p.L = P->geom.Kd[P->geom.ndim - 1];
-    p.nin = nin;
-    p.nout = nout;
-    p.tw = static_cast<const float2*>(P->colfft_tw.p);
+    p.in = static_cast<const float2*>(a.in);
+    p.out = static_cast<float2*>(a.out);
+    p.S = a.S;
+    p.ps = a.ps;
+    p.ps2 = a.ps2;
+    p.planes = a.planes;
+    p.planes2 = a.planes2;
+    p.L = P->geom.Kd[a.axis];
+    p.nin = a.nin;
+    p.nout = a.nout;
+    p.tw = static_cast<const float2*>(P->fft_tw[a.axis].p);
     p.check = static_cast<unsigned*>(P->check.p);
-    p.in_elems = in_elems;
-    p.out_elems = out_elems;
-    GBN_CUDA(launch_colfft(p, sign, s), "last-axis FFT pass");
+    p.in_elems = a.in_elems;
+    p.out_elems = a.out_elems;
+    GBN_CUDA(launch_colfft(p, sign, s), "strided-axis FFT pass");
     return GBN_OK;
 }
 
@@ -861,12 +878,43 @@ int exec_fft(gbn_plan* P, cufftHandle h, void* in, void* out, int dir, cudaStrea
 // 2-D last-axis pass: forward mid -> grid (the N_1 slabs with data read),
 // inverse grid -> grid in place (the N_1 slabs the crop reads written).
 int colfft_2d(gbn_plan* P, int planes, int sign, cudaStream_t s) {
-    const int64_t S = (int64_t)planes * P->geom.Kd[0];
     const int64_t ge = (int64_t)P->cap_planes * P->Kprod;
-    if (sign < 0)
-        return run_colfft(P, P->mid.p, (int64_t)P->mid_planes * P->Kprod, P->grid.p, ge, S, 0, 1, last_n(P),
-                          P->geom.Kd[1], -1, s);
-    return run_colfft(P, P->grid.p, ge, P->grid.p, ge, S, 0, 1, P->geom.Kd[1], last_n(P), 1, s);
+    AxisPass a{P->grid.p, ge, P->grid.p, ge, 1, (int64_t)planes * P->geom.Kd[0], 0, 0, 1, 1,
+               P->geom.Kd[1], last_n(P)};
+    if (sign < 0) {
+        a.in = P->mid.p;
+        a.in_elems = (int64_t)P->mid_planes * P->Kprod;
+        a.nin = last_n(P);
+        a.nout = P->geom.Kd[1];
+    }
+    return run_colfft(P, a, sign, s);
+}
+
+// 3-D passes along axes 1 and 2 of the grid, in place: forward axis 1 over
+// the N_2 z-slabs with data (N_1 rows read), then axis 2 (N_2 z-slabs read);
+// inverse axis 2 (N_2 z-slabs written), then axis 1 over those slabs (N_1
+// rows written).
+int colfft_3d(gbn_plan* P, int planes, int sign, cudaStream_t s) {
+    const gbn_geometry& G = P->geom;
+    const int64_t ge = (int64_t)P->cap_planes * P->Kprod;
+    const int64_t slab = (int64_t)G.Kd[0] * G.Kd[1];
+    AxisPass a1{P->grid.p, ge, P->grid.p, ge, 1, G.Kd[0], slab, P->Kprod, G.Nd[2], planes, 0, 0};
+    AxisPass a2{P->grid.p, ge, P->grid.p, ge, 2, slab, P->Kprod, 0, planes, 1, 0, 0};
+    int rc;
+    if (sign < 0) {
+        a1.nin = G.Nd[1];
+        a1.nout = G.Kd[1];
+        a2.nin = G.Nd[2];
+        a2.nout = G.Kd[2];
+        if ((rc = run_colfft(P, a1, -1, s))) return rc;
+        return run_colfft(P, a2, -1, s);
+    }
+    a2.nin = G.Kd[2];
+    a2.nout = G.Nd[2];
+    a1.nin = G.Kd[1];
+    a1.nout = G.Nd[1];
+    if ((rc = run_colfft(P, a2, 1, s))) return rc;
+    return run_colfft(P, a1, 1, s);
 }
 
 // Forward Kd-point FFT of the padded planes into the grid.  2-D and 3-D:
@@ -886,8 +934,11 @@ int fft_forward(gbn_plan* P, int planes, cudaStream_t s) {
         for (int pl = 0; pl < planes; ++pl)
             if ((rc = exec_fft(P, f->hx, pad + pl * pb, mid + pl * pb, CUFFT_FORWARD, s))) return rc;
         if (P->colfft)
-            return run_colfft(P, mid, (int64_t)P->mid_planes * P->Kprod, grid, (int64_t)P->cap_planes * P->Kprod,
-                              slab_cells(P), P->Kprod, planes, last_n(P), P->geom.Kd[2], -1, s);
+            return run_colfft(P,
+                              AxisPass{mid, (int64_t)P->mid_planes * P->Kprod, grid,
+                                       (int64_t)P->cap_planes * P->Kprod, 2, slab_cells(P), P->Kprod, 0, planes,
+                                       1, last_n(P), P->geom.Kd[2]},
+                              -1, s);
         for (int pl = 0; pl < planes; ++pl)
             if ((rc = exec_fft(P, f->hy, mid + pl * pb, grid + pl * pb, CUFFT_FORWARD, s))) return rc;
         return GBN_OK;
@@ -932,7 +983,8 @@ int fft_inverse(gbn_plan* P, int planes, cudaStream_t s) {
         char* grid = static_cast<char*>(P->grid.p);
         if (P->colfft) {
             const int64_t ge = (int64_t)P->cap_planes * P->Kprod;
-            if ((rc = run_colfft(P, grid, ge, grid, ge, slab_cells(P), P->Kprod, planes, P->geom.Kd[2], last_n(P),
+            if ((rc = run_colfft(P, AxisPass{grid, ge, grid, ge, 2, slab_cells(P), P->Kprod, 0, planes, 1,
+                                             P->geom.Kd[2], last_n(P)},
                                  1, s)))
                 return rc;
         } else {
@@ -1103,7 +1155,7 @@ int run_spread_noalloc(gbn_plan* P, const void* y, void* grid, int coils, cudaSt
 
 template <typename R>
 int run_forward(gbn_plan* P, const void* x, void* y, int coils, cudaStream_t s, const void* maps = nullptr) {
-    int rc = ensure_buffers(P, coils);
+    int rc = ensure_buffers(P, coils, P->rowfft && !maps);
     if (rc) return rc;
     if (!P->pad.p || !P->grid.p) return fail(GBN_ERR_NOMEM, "transform buffers missing");
     const gbn_geometry& G = P->geom;
@@ -1127,13 +1179,16 @@ int run_forward(gbn_plan* P, const void* x, void* y, int coils, cudaStream_t s, 
     pp.out_elems = (int64_t)P->cap_planes * P->Kprod;
     internal_layout(P, P->F * coils, pp);
     if (P->rowfft && !maps) {
-        // single precision only (rowfft is off for double plans)
+        // single precision only (rowfft is off for double plans); 2-D rows
+        // into mid, 3-D rows into the grid, whose passes run in place
         {
             NvtxRange r("gbn forward: pad + fft");
-            if ((rc = run_rowfft(P, x, pp.x_elems, P->mid.p, (int64_t)P->mid_planes * P->Kprod, P->F * coils, -1,
-                                 s)))
+            const int planes = P->F * coils;
+            const bool d2 = G.ndim == 2;
+            if ((rc = run_rowfft(P, x, pp.x_elems, d2 ? P->mid.p : P->grid.p,
+                                 (int64_t)(d2 ? P->mid_planes : P->cap_planes) * P->Kprod, planes, -1, s)))
                 return rc;
-            if ((rc = colfft_2d(P, P->F * coils, -1, s))) return rc;
+            if ((rc = d2 ? colfft_2d(P, planes, -1, s) : colfft_3d(P, planes, -1, s))) return rc;
         }
         NvtxRange r("gbn forward: gather");
         return run_gather<R>(P, P->grid.p, y, coils, true, s);
@@ -1154,7 +1209,7 @@ template <typename R>
 int run_adjoint(gbn_plan* P, const void* y, void* x, int coils, cudaStream_t s, const void* maps = nullptr) {
     // allocate first: the grid pointer handed to the spread must be the
     // buffer this call will use (it is null before the first call)
-    int rc = ensure_buffers(P, coils);
+    int rc = ensure_buffers(P, coils, P->rowfft && !maps);
     if (rc) return rc;
     if (!P->grid.p) return fail(GBN_ERR_NOMEM, "grid buffer missing");
     {
@@ -1164,7 +1219,8 @@ int run_adjoint(gbn_plan* P, const void* y, void* x, int coils, cudaStream_t s, 
     }
     if (P->rowfft && !maps) {
         NvtxRange r("gbn adjoint: fft + crop");
-        if ((rc = colfft_2d(P, P->F * coils, 1, s))) return rc;
+        if ((rc = P->geom.ndim == 2 ? colfft_2d(P, P->F * coils, 1, s) : colfft_3d(P, P->F * coils, 1, s)))
+            return rc;
         return run_rowfft(P, P->grid.p, (int64_t)P->cap_planes * P->Kprod, x, (int64_t)P->F * coils * P->Nprod,
                           P->F * coils, 1, s);
     }

@@ -1,16 +1,17 @@
-// Row passes of the 2-D oversampled FFT with the deapodisation, zero-pad and
-// crop folded in.
+// Row passes of the 2-D and 3-D oversampled FFTs with the deapodisation,
+// zero-pad and crop folded in.
 //
 // Forward (mrrt/nufft/_nufft.py:1325-1331, then the first axis of fftn): each
-// image row x[plane][n1][:N0] is multiplied by sn[n1][:N0], taken as the first
-// N0 of K0 values (the rest zero, never stored or read) and transformed along
-// memory axis 0 into its slab of the row-interleaved grid (slab offset
-// plane * gsp + n1 * gs1).  This replaces the pad kernel's write of the
-// zero-padded planes and the row FFT's read of them.
-// Inverse (the first axis of ifftn, then :1561-1572): each slab row the crop
-// keeps (n1 < N1) is transformed back and only its first N0 outputs are
-// formed into the image, scaled by scale * sn: the row FFT's write and the
-// crop's read of the transformed rows are gone.
+// image row x[plane][n2][n1][:N0] is multiplied by sn[n2][n1][:N0], taken as
+// the first N0 of K0 values (the rest zero, never stored or read) and
+// transformed along memory axis 0 into its grid row (offset plane * gsp +
+// n2 * gs2 + n1 * gs1: the row-interleaved 2-D grid or the plane-major 3-D
+// grid).  This replaces the pad kernel's write of the zero-padded planes and
+// the row FFT's read of them.
+// Inverse (the first axis of ifftn, then :1561-1572): each grid row the crop
+// keeps (n1 < N1, n2 < N2) is transformed back and only its first N0 outputs
+// are formed into the image, scaled by scale * sn: the row FFT's write and
+// the crop's read of the transformed rows are gone.
 //
 // Same four-step split as the last-axis pass (gbn_colfft.cu), with a CTA
 // owning TR whole rows: step A thread (row, n1) loads elements n1 + L1 n2 of
@@ -31,14 +32,17 @@ namespace gbn {
 
 namespace {
 
-template <int L1, int L2, int TR, int SIGN>
+// D3: rows of a 3-D image (N2 > 1; a separate instantiation keeps the 2-D
+// kernel's row arithmetic to one division).
+template <int L1, int L2, int TR, int SIGN, bool D3>
 __global__ void __launch_bounds__(TR * L1) rowfft_kernel(const RowFftParams p) {
     constexpr int LP = L1 + 1;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float2* sm = reinterpret_cast<float2*>(smem_raw);
-    const int64_t rows = (int64_t)p.planes * p.N1;
+    const int64_t rpp = D3 ? (int64_t)p.N1 * p.N2 : p.N1;   // rows per plane
+    const int64_t rows = (int64_t)p.planes * rpp;
     const int64_t r0 = (int64_t)blockIdx.x * TR;
-    const int64_t Nprod = (int64_t)p.N0 * p.N1;
+    const int64_t Nprod = rpp * p.N0;
 
     // step A: (row, n1), L2-point transforms of elements n1 + L1 n2
     {
@@ -48,12 +52,12 @@ __global__ void __launch_bounds__(TR * L1) rowfft_kernel(const RowFftParams p) {
 #pragma unroll
         for (int n2 = 0; n2 < L2; ++n2) v[n2] = make_float2(0.f, 0.f);
         if (r < rows) {
-            const int64_t pl = r / p.N1;
-            const int row = (int)(r - pl * p.N1);
+            const int64_t pl = r / rpp;
+            const int rr = (int)(r - pl * rpp);   // image row within the plane
             if (SIGN < 0) {
                 // image row times sn, zero past N0
-                const int64_t xo = pl * Nprod + (int64_t)row * p.N0;
-                const float* s = p.sn + (int64_t)row * p.N0;
+                const int64_t xo = pl * Nprod + (int64_t)rr * p.N0;
+                const float* s = p.sn + (int64_t)rr * p.N0;
 #pragma unroll
                 for (int n2 = 0; n2 < L2; ++n2) {
                     const int n = n1 + L1 * n2;
@@ -64,7 +68,8 @@ __global__ void __launch_bounds__(TR * L1) rowfft_kernel(const RowFftParams p) {
                     }
                 }
             } else {
-                const int64_t go = pl * p.gsp + (int64_t)row * p.gs1;
+                const int n2r = D3 ? rr / p.N1 : 0;
+                const int64_t go = pl * p.gsp + (int64_t)n2r * p.gs2 + (int64_t)(rr - n2r * p.N1) * p.gs1;
 #pragma unroll
                 for (int n2 = 0; n2 < L2; ++n2) {
                     const int n = n1 + L1 * n2;
@@ -92,10 +97,11 @@ __global__ void __launch_bounds__(TR * L1) rowfft_kernel(const RowFftParams p) {
         for (int n1 = 0; n1 < L1; ++n1) u[n1] = sm[(rl * L2 + k2) * LP + n1];
         stockham<L1, 1, SIGN>(u);
         if (r >= rows) continue;
-        const int64_t pl = r / p.N1;
-        const int row = (int)(r - pl * p.N1);
+        const int64_t pl = r / rpp;
+        const int rr = (int)(r - pl * rpp);
         if (SIGN < 0) {
-            const int64_t go = pl * p.gsp + (int64_t)row * p.gs1;
+            const int n2r = D3 ? rr / p.N1 : 0;
+            const int64_t go = pl * p.gsp + (int64_t)n2r * p.gs2 + (int64_t)(rr - n2r * p.N1) * p.gs1;
 #pragma unroll
             for (int k1 = 0; k1 < L1; ++k1) {
                 const int k = k2 + L2 * k1;
@@ -103,8 +109,8 @@ __global__ void __launch_bounds__(TR * L1) rowfft_kernel(const RowFftParams p) {
             }
         } else {
             // the crop: first N0 outputs, times scale, times sn
-            const int64_t xo = pl * Nprod + (int64_t)row * p.N0;
-            const float* s = p.sn + (int64_t)row * p.N0;
+            const int64_t xo = pl * Nprod + (int64_t)rr * p.N0;
+            const float* s = p.sn + (int64_t)rr * p.N0;
 #pragma unroll
             for (int k1 = 0; k1 < L1; ++k1) {
                 const int k = k2 + L2 * k1;
@@ -123,16 +129,23 @@ __global__ void __launch_bounds__(TR * L1) rowfft_kernel(const RowFftParams p) {
 template <int L1, int L2, int TR>
 cudaError_t rowfft_launch(const RowFftParams& p, int sign, cudaStream_t s) {
     const size_t smem = (size_t)TR * L2 * (L1 + 1) * sizeof(float2);
-    const void* k = sign < 0 ? reinterpret_cast<const void*>(rowfft_kernel<L1, L2, TR, -1>)
-                             : reinterpret_cast<const void*>(rowfft_kernel<L1, L2, TR, 1>);
+    const bool d3 = p.N2 > 1;
+    const void* k = sign < 0 ? (d3 ? reinterpret_cast<const void*>(rowfft_kernel<L1, L2, TR, -1, true>)
+                                   : reinterpret_cast<const void*>(rowfft_kernel<L1, L2, TR, -1, false>))
+                             : (d3 ? reinterpret_cast<const void*>(rowfft_kernel<L1, L2, TR, 1, true>)
+                                   : reinterpret_cast<const void*>(rowfft_kernel<L1, L2, TR, 1, false>));
     cudaError_t e = ensure_dynamic_smem(k, smem);
     if (e != cudaSuccess) return e;
-    const int64_t ctas = ((int64_t)p.planes * p.N1 + TR - 1) / TR;
+    const int64_t ctas = ((int64_t)p.planes * p.N1 * p.N2 + TR - 1) / TR;
     if (ctas > INT32_MAX) return cudaErrorInvalidValue;
-    if (sign < 0)
-        rowfft_kernel<L1, L2, TR, -1><<<(unsigned)ctas, TR * L1, smem, s>>>(p);
+    if (sign < 0 && d3)
+        rowfft_kernel<L1, L2, TR, -1, true><<<(unsigned)ctas, TR * L1, smem, s>>>(p);
+    else if (sign < 0)
+        rowfft_kernel<L1, L2, TR, -1, false><<<(unsigned)ctas, TR * L1, smem, s>>>(p);
+    else if (d3)
+        rowfft_kernel<L1, L2, TR, 1, true><<<(unsigned)ctas, TR * L1, smem, s>>>(p);
     else
-        rowfft_kernel<L1, L2, TR, 1><<<(unsigned)ctas, TR * L1, smem, s>>>(p);
+        rowfft_kernel<L1, L2, TR, 1, false><<<(unsigned)ctas, TR * L1, smem, s>>>(p);
     return cudaGetLastError();
 }
 
@@ -147,7 +160,7 @@ bool rowfft_supported(int L) { return colfft_supported(L); }
 //   384, 512 planes x 192 rows: 16 x 24 with 8 rows 99.7 + 110.1 us, 16 rows
 //     100.2 + 117.5 us (cuFFT's row pass alone 161.5 us).
 cudaError_t launch_rowfft(const RowFftParams& p, int sign, cudaStream_t s) {
-    if (p.planes <= 0 || p.N1 <= 0 || p.N0 <= 0 || p.N0 > p.L) return cudaErrorInvalidValue;
+    if (p.planes <= 0 || p.N1 <= 0 || p.N2 <= 0 || p.N0 <= 0 || p.N0 > p.L) return cudaErrorInvalidValue;
     switch (p.L) {
         case 64: return rowfft_launch<8, 8, 16>(p, sign, s);
         case 96: return rowfft_launch<8, 12, 16>(p, sign, s);

@@ -120,3 +120,17 @@ def test_2d_fused_row_passes_orthonormal_scaling(gpu_lib):
     ys, xs = _run(plans, 2, 1)
     assert rel_l2(ys[0], ys[1]) < TOL
     assert rel_l2(xs[0], xs[1]) < TOL
+
+
+@pytest.mark.parametrize("N,K,coils,frames", [
+    ((32, 32, 32), (64, 64, 64), 2, 1),
+    ((40, 30, 50), (96, 64, 128), 2, 1),
+    ((20, 24, 16), (64, 96, 64), 3, 6),     # 18 planes: past the per-plane cuFFT path's limit
+])
+def test_3d_all_passes_on_own_kernels(gpu_lib, N, K, coils, frames):
+    """Every axis supported: rows with the pad / crop folded in, then axes 1
+    and 2 in place on the grid."""
+    plans = _pair(N, K, (4, 4, 4), coils=coils, frames=frames, M=800, seed=sum(N))
+    ys, xs = _run(plans, coils, frames)
+    assert rel_l2(ys[0], ys[1]) < TOL
+    assert rel_l2(xs[0], xs[1]) < TOL
