@@ -24,7 +24,7 @@ BUILD_CHECKED = os.path.join(HERE, "_build_checked")
 LIB_CHECKED_PATH = os.path.join(HERE, "libgbnufft_checked.so")
 
 SOURCES = ["gbn_plan.cu", "gbn_gather.cu", "gbn_spread.cu", "gbn_padcrop.cu", "gbn_dtft.cu", "gbn_grad.cu",
-           "gbn_noalloc.cu", "gbn_coef.cu", "gbn_hostio.cu", "gbn_bin.cu", "gbn_sort.cu", "gbn_colfft.cu", "gbn_rowfft.cu"]
+           "gbn_noalloc.cu", "gbn_coef.cu", "gbn_bin.cu", "gbn_sort.cu", "gbn_colfft.cu", "gbn_rowfft.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 

@@ -351,9 +351,4 @@ cudaError_t launch_dtft(bool adjoint, int ndim, const int* Nd, const double* n_s
                         const double* omega, int64_t M, const double2* in, double2* out,
                         int reps, cudaStream_t s);
 
-// Copy of `bytes` (16-byte multiple, both pointers 16-byte aligned) from
-// host memory the device reads in place (pageable memory on a device with
-// cudaDevAttrPageableMemoryAccess) to device memory, by a kernel on `s`.
-cudaError_t launch_host_read(void* dst, const void* src, size_t bytes, int sms, cudaStream_t s);
-
 }  // namespace gbn

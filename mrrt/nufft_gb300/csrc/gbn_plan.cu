@@ -164,8 +164,6 @@ struct HostIo {
     cudaStream_t h2d = nullptr, d2h = nullptr;
     std::vector<cudaEvent_t> ev;
     DevBuf in, out;
-    int pageable = -1;   // the device reads pageable host memory in place
-    int sms = 0;
     ~HostIo() {
         for (cudaEvent_t e : ev) cudaEventDestroy(e);
         if (h2d) cudaStreamDestroy(h2d);
@@ -1264,7 +1262,13 @@ int run_adjoint(gbn_plan* P, const void* y, void* x, int coils, cudaStream_t s, 
 // stream, each waiting for its chunk's transform.  So chunk k is transformed
 // while chunk k + 1 is copied in and chunk k - 1 copied out.  16 coils keep
 // the batched kernels efficient (half the batch costs 0.6-0.7 of the full
-// one) while halving the exposed copy at each end.
+// one) while halving the exposed copy at each end; the forward starts with
+// two 8-coil chunks, since its output (the samples, 3x the image at the 2-D
+// workload) is the longer copy and starts sooner (forward 0.477 -> 0.459 ms
+// at 32 coils).  Every copy runs on the copy engines, pageable memory too:
+// reading pageable input with SM loads (the device can, over NVLink-C2C) ran
+// at the same 203 GB/s but took SMs from the transforms (0.491 against
+// 0.477 ms).
 constexpr int HOST_CHUNK = 16;
 
 int host_io_init(gbn_plan* P, int nev) {
@@ -1275,14 +1279,6 @@ int host_io_init(gbn_plan* P, int nev) {
         cudaEvent_t e;
         GBN_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "copy event");
         h.ev.push_back(e);
-    }
-    if (h.pageable < 0) {
-        int v = 0;
-        if (cudaDeviceGetAttribute(&v, cudaDevAttrPageableMemoryAccess, P->device) != cudaSuccess) v = 0;
-        int n = 0;
-        GBN_CUDA(cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, P->device), "SM count");
-        h.sms = n;
-        h.pageable = v;
     }
     return GBN_OK;
 }
@@ -1309,8 +1305,20 @@ int run_host(gbn_plan* P, bool forward, const void* in, void* out, int coils, cu
     const size_t csz = (size_t)2 * P->rsize;
     const size_t img = (size_t)P->F * P->Nprod * csz, smp = (size_t)P->M_total * csz;   // per coil
     const size_t in_per = forward ? img : smp, out_per = forward ? smp : img;
-    const int chunk = (P->F == 1 && coils >= 2 * HOST_CHUNK) ? HOST_CHUNK : coils;
-    const int nchunks = (coils + chunk - 1) / chunk;
+    // chunk k covers coils [cstart[k], cstart[k + 1])
+    std::vector<int> cstart{0};
+    if (P->F == 1 && coils >= 2 * HOST_CHUNK) {
+        // the forward's first two chunks are half size: its output (the
+        // samples) starts copying out sooner
+        while (cstart.back() < coils) {
+            const int k = (int)cstart.size() - 1;
+            const int want = (forward && k < 2) ? HOST_CHUNK / 2 : HOST_CHUNK;
+            cstart.push_back(std::min(coils, cstart.back() + want));
+        }
+    } else {
+        cstart.push_back(coils);
+    }
+    const int nchunks = (int)cstart.size() - 1;
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
     GBN_CUDA(cudaStreamIsCapturing(s, &cs), "capture status");
     if (cs != cudaStreamCaptureStatusNone)
@@ -1324,8 +1332,6 @@ int run_host(gbn_plan* P, bool forward, const void* in, void* out, int coils, cu
     // staging is idle here: every host-buffer call waits for its copies
     if ((rc = grow(h.in, in_per * coils, "host input staging allocation failed"))) return rc;
     if ((rc = grow(h.out, out_per * coils, "host output staging allocation failed"))) return rc;
-    const bool read_in_place = kin == cudaMemoryTypeUnregistered && h.pageable == 1 &&
-                               (reinterpret_cast<uintptr_t>(in) & 15) == 0 && in_per % 16 == 0;
     char* din = static_cast<char*>(h.in.p);
     char* dout = static_cast<char*>(h.out.p);
     cudaEvent_t* ev = h.ev.data();
@@ -1335,13 +1341,11 @@ int run_host(gbn_plan* P, bool forward, const void* in, void* out, int coils, cu
     GBN_CUDA(cudaStreamWaitEvent(h.d2h, ev[0], 0), "stream wait");
     int issued = 0;
     for (int k = 0; k < nchunks && rc == GBN_OK; ++k) {
-        const int c0 = k * chunk, n = std::min(chunk, coils - c0);
+        const int c0 = cstart[k], n = cstart[k + 1] - c0;
         const size_t off = (size_t)c0 * in_per, bytes = (size_t)n * in_per;
         cudaError_t e = cudaSuccess;
         if (bytes)
-            e = read_in_place ? launch_host_read(din + off, static_cast<const char*>(in) + off, bytes, h.sms, h.h2d)
-                              : cudaMemcpyAsync(din + off, static_cast<const char*>(in) + off, bytes,
-                                                cudaMemcpyHostToDevice, h.h2d);
+            e = cudaMemcpyAsync(din + off, static_cast<const char*>(in) + off, bytes, cudaMemcpyHostToDevice, h.h2d);
         if (e == cudaSuccess) e = cudaEventRecord(ev[1 + 2 * k], h.h2d);
         if (e == cudaSuccess) e = cudaStreamWaitEvent(s, ev[1 + 2 * k], 0);
         if (e != cudaSuccess) {
@@ -1357,7 +1361,7 @@ int run_host(gbn_plan* P, bool forward, const void* in, void* out, int coils, cu
         issued = k + 1;
     }
     for (int k = 0; k < issued && rc == GBN_OK; ++k) {
-        const int c0 = k * chunk, n = std::min(chunk, coils - c0);
+        const int c0 = cstart[k], n = cstart[k + 1] - c0;
         const size_t off = (size_t)c0 * out_per, bytes = (size_t)n * out_per;
         cudaError_t e = cudaStreamWaitEvent(h.d2h, ev[2 + 2 * k], 0);
         if (e == cudaSuccess && bytes)
