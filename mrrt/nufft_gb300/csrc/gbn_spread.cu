@@ -152,6 +152,7 @@ spread_kernel(const SpreadParams<R> p) {
     // CTAs taking work tickets as the 3-D gather does, measured slower here:
     // 0.191 against 0.151 ms at the 2-D 32-coil workload, 5.78 against
     // 5.71 ms at the 3-D kooshball.)
+    __shared__ unsigned char hitpos[8][32];   // per warp: positions of the current group's hits
     const int item = blockIdx.x, chunk = blockIdx.y;
     const int4 it = p.items[item];
     const int2 part = p.parts[item];
@@ -316,17 +317,33 @@ spread_kernel(const SpreadParams<R> p) {
                 if (NDIM > 2) hit = hit && s.z < bo2 + B2 && s.z + Jz > bo2;
             }
             unsigned mask = __ballot_sync(0xffffffffu, hit);
-            while (mask) {
-                // slot k takes the k-th and (k + SW)-th remaining hits and
-                // accumulates them in entry order: two independent load
-                // chains in flight per iteration
-                int pos = -1;
-                for (int kk = 0; kk < SW && mask; ++kk) {
-                    const int pk = __ffs(mask) - 1;
-                    mask &= mask - 1;
-                    if (kk == slot) pos = pk;
+            if (SW > 1) {
+                // several samples per warp: the hits' positions are compacted
+                // into this warp's list, and slot k takes hits k, k + SW,
+                // k + 2 SW, ... in entry order (the order, hence the sums, of
+                // a serial pick)
+                if (hit) hitpos[warp][__popc(mask & ((1u << lane) - 1u))] = (unsigned char)lane;
+                __syncwarp();
+                const int nh = __popc(mask);
+                for (int r = slot; r < nh; r += SW) {
+                    const int pos = hitpos[warp][r];
+                    if (coil < nc) {
+                        EntryOps<R, NDIM, CX, SL, ROWSKIP> A;
+                        A.load(cp, vb, sls, gb + pos, VS, coil, bo0, bo1, bo2);
+                        if (ROWSKIP) {
+                            A.ry = sls[gb + pos].y - bo1;
+                            A.Jy = Jy;
+                        }
+                        A.accumulate(acc);
+                    }
                 }
-                if (pos >= 0 && coil < nc) {
+                __syncwarp();   // the list is rewritten for the next group
+                continue;
+            }
+            while (mask) {
+                const int pos = __ffs(mask) - 1;
+                mask &= mask - 1;
+                if (coil < nc) {
                     EntryOps<R, NDIM, CX, SL, ROWSKIP> A;
                     A.load(cp, vb, sls, gb + pos, VS, coil, bo0, bo1, bo2);
                     if (ROWSKIP) {
