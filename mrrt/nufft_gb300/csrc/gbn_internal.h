@@ -134,6 +134,8 @@ struct SpreadParams {
     int apply_pb;
     int apply_ph;
     int chunks;                     // coil chunks of LS lanes (gridDim.y)
+    int cpf;                        // set by the launcher: precomputed coefficients prefetched
+                                    // into shared memory a chunk ahead
 };
 
 template <typename R>

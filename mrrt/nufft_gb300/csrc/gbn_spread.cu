@@ -28,6 +28,10 @@ namespace gbn {
 
 __host__ __device__ constexpr int cpad_len(int B) { return ((2 * (B - 1) + JMAX + 3) / 4) * 4; }
 
+// Shared memory per CTA up to which the coefficient prefetch is used: four
+// CTAs of it fit an SM's 228 KB.
+constexpr size_t SPREAD_CPF_SMEM = 56 * 1024;
+
 template <int NDIM>
 struct SpreadLayout {
     static constexpr int B0 = SpreadBlock<NDIM>::B0, B1 = SpreadBlock<NDIM>::B1, B2 = SpreadBlock<NDIM>::B2;
@@ -143,10 +147,13 @@ spread_kernel(const SpreadParams<R> p) {
     //                     multiply applies c to re and im at once),
     //                     (Re c, -Im c) = conj(c) for a complex kernel
     //   tb[2][NDIM][CH]   coordinates, lsb[2][CH] window starts
+    //   craw[2][CX ? 2 : 1][CH * jsum]  (cpf) the chunk's precomputed
+    //                     coefficients as stored, copied in with its values
     C* vbuf = reinterpret_cast<C*>(smem_raw);
     C* cp = vbuf + 2 * CH * VS;
     short4* lsb = reinterpret_cast<short4*>(cp + CH * SL::PSTR);
     R* tb = reinterpret_cast<R*>(lsb + 2 * CH);
+    R* craw = tb + 2 * NDIM * CH;
 
     // One CTA per (work item, coil chunk).  (A persistent launch, resident
     // CTAs taking work tickets as the 3-D gather does, measured slower here:
@@ -242,6 +249,16 @@ spread_kernel(const SpreadParams<R> p) {
                     cp_async<sizeof(R)>(tb + (b * NDIM + d) * CH + q, p.s.t[d] + e0 + q);
             }
         }
+        if (p.cpf) {
+            // the chunk's coefficients, contiguous in list order
+            const int nq = n * p.s.jsum;
+            R* dst = craw + (size_t)b * (CX ? 2 : 1) * CH * p.s.jsum;
+            const R* src = p.s.cr + (int64_t)e0 * p.s.jsum;
+            for (int q = tid; q < nq; q += nthr) {
+                cp_async<sizeof(R)>(dst + q, src + q);
+                if (CX) cp_async<sizeof(R)>(dst + CH * p.s.jsum + q, p.s.ci + (int64_t)e0 * p.s.jsum + q);
+            }
+        }
         cp_async_commit();
     };
 
@@ -288,7 +305,11 @@ spread_kernel(const SpreadParams<R> p) {
                 }
             }
             R cr, ci = (R)0;
-            if (p.s.cr) {
+            if (p.cpf) {
+                const R* raw = craw + (size_t)b * (CX ? 2 : 1) * CH * Jsum;
+                cr = raw[q];
+                if (CX) ci = raw[CH * Jsum + q];
+            } else if (p.s.cr) {
                 const int64_t ce = (int64_t)(start + k * CH + el) * Jsum + (q - el * Jsum);
                 cr = p.s.cr[ce];
                 if (CX) ci = p.s.ci[ce];
@@ -519,8 +540,16 @@ static cudaError_t ensure_smem(K kernel, size_t bytes) {
 }
 
 template <typename R, int NDIM, bool CX, int JJ, int LSC, bool ROWSKIP = false>
-static cudaError_t spread_launch(const SpreadParams<R>& p, cudaStream_t s) {
-    const size_t smem = spread_smem(p.g, p.ln);
+static cudaError_t spread_launch(const SpreadParams<R>& p0, cudaStream_t s) {
+    // Precomputed coefficients are copied into shared memory a chunk ahead
+    // (cp.async, with the values) when the extra buffer still leaves four
+    // CTAs per SM; otherwise the row staging reads them from global memory
+    // between the chunk's barriers.
+    SpreadParams<R> p = p0;
+    const size_t base = spread_smem(p.g, p.ln);
+    const size_t raw = p.s.cr ? 2 * (size_t)(CX ? 2 : 1) * SPREAD_CHUNK_ENTRIES * p.s.jsum * sizeof(R) : 0;
+    p.cpf = p.s.cr && base + raw <= SPREAD_CPF_SMEM;
+    const size_t smem = base + (p.cpf ? raw : 0);
     cudaError_t e = ensure_smem(spread_kernel<R, NDIM, CX, JJ, LSC, ROWSKIP>, smem);
     if (e != cudaSuccess) return e;
     const int threads = spread_threads(NDIM, p.g.T);
