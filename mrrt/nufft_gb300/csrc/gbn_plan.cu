@@ -29,7 +29,9 @@ using namespace gbn;
 namespace gbn {
 
 cudaError_t ensure_dynamic_smem(const void* kernel, size_t bytes) {
-    if (bytes <= 48 * 1024) return cudaSuccess;
+    // without the attribute a launch may use 48 KB of shared memory, static
+    // and dynamic together
+    if (bytes <= 40 * 1024) return cudaSuccess;
     struct Entry { const void* k; int dev; size_t bytes; };
     static std::mutex mu;
     static std::vector<Entry> done;
@@ -39,8 +41,13 @@ cudaError_t ensure_dynamic_smem(const void* kernel, size_t bytes) {
     std::lock_guard<std::mutex> lk(mu);
     for (auto& x : done)
         if (x.k == kernel && x.dev == dev && x.bytes >= bytes) return cudaSuccess;
-    e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    cudaFuncAttributes fa;
+    e = cudaFuncGetAttributes(&fa, kernel);
     if (e != cudaSuccess) return e;
+    if (bytes + fa.sharedSizeBytes > 48 * 1024) {
+        e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+        if (e != cudaSuccess) return e;
+    }
     for (auto& x : done)
         if (x.k == kernel && x.dev == dev) {
             x.bytes = bytes;

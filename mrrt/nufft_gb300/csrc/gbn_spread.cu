@@ -147,8 +147,8 @@ spread_kernel(const SpreadParams<R> p) {
     //                     multiply applies c to re and im at once),
     //                     (Re c, -Im c) = conj(c) for a complex kernel
     //   tb[2][NDIM][CH]   coordinates, lsb[2][CH] window starts
-    //   craw[2][CX ? 2 : 1][CH * jsum]  (cpf) the chunk's precomputed
-    //                     coefficients as stored, copied in with its values
+    //   craw[CX ? 2 : 1][CH * jsum]  (cpf) the next chunk's precomputed
+    //                     coefficients as stored, copied in beside its values
     C* vbuf = reinterpret_cast<C*>(smem_raw);
     C* cp = vbuf + 2 * CH * VS;
     short4* lsb = reinterpret_cast<short4*>(cp + CH * SL::PSTR);
@@ -249,22 +249,25 @@ spread_kernel(const SpreadParams<R> p) {
                     cp_async<sizeof(R)>(tb + (b * NDIM + d) * CH + q, p.s.t[d] + e0 + q);
             }
         }
-        if (p.cpf) {
-            // the chunk's coefficients, contiguous in list order
-            const int nq = n * p.s.jsum;
-            R* dst = craw + (size_t)b * (CX ? 2 : 1) * CH * p.s.jsum;
-            const R* src = p.s.cr + (int64_t)e0 * p.s.jsum;
-            for (int q = tid; q < nq; q += nthr) {
-                cp_async<sizeof(R)>(dst + q, src + q);
-                if (CX) cp_async<sizeof(R)>(dst + CH * p.s.jsum + q, p.s.ci + (int64_t)e0 * p.s.jsum + q);
-            }
+    };
+    // (cpf) the chunk's coefficients, contiguous in list order, into the one
+    // raw buffer: issued once the previous chunk's rows are built
+    auto issue_coefs = [&](int chunk) {
+        if (!p.cpf) return;
+        const int n = min(CH, count - chunk * CH);
+        const int64_t e0 = (int64_t)start + chunk * CH;
+        const int nq = n * p.s.jsum;
+        for (int q = tid; q < nq; q += nthr) {
+            cp_async<sizeof(R)>(craw + q, p.s.cr + e0 * p.s.jsum + q);
+            if (CX) cp_async<sizeof(R)>(craw + CH * p.s.jsum + q, p.s.ci + e0 * p.s.jsum + q);
         }
-        cp_async_commit();
     };
 
     if (nchunks > 0) {
         load_meta(0);
         issue(0, 0);
+        issue_coefs(0);
+        cp_async_commit();
 #pragma unroll
         for (int u = 0; u < 2; ++u) cph[u] = nph[u];
         load_meta(1);
@@ -306,9 +309,8 @@ spread_kernel(const SpreadParams<R> p) {
             }
             R cr, ci = (R)0;
             if (p.cpf) {
-                const R* raw = craw + (size_t)b * (CX ? 2 : 1) * CH * Jsum;
-                cr = raw[q];
-                if (CX) ci = raw[CH * Jsum + q];
+                cr = craw[q];
+                if (CX) ci = craw[CH * Jsum + q];
             } else if (p.s.cr) {
                 const int64_t ce = (int64_t)(start + k * CH + el) * Jsum + (q - el * Jsum);
                 cr = p.s.cr[ce];
@@ -327,6 +329,9 @@ spread_kernel(const SpreadParams<R> p) {
             load_meta(k + 2);
         }
         __syncthreads();
+        // every row of chunk k is built: the raw buffer takes chunk k+1's
+        if (k + 1 < nchunks) issue_coefs(k + 1);
+        cp_async_commit();
         // ---- accumulate: each warp takes the entries touching its block --------
         for (int gb = 0; gb < n; gb += 32) {
             const int l = gb + lane;
@@ -547,7 +552,7 @@ static cudaError_t spread_launch(const SpreadParams<R>& p0, cudaStream_t s) {
     // between the chunk's barriers.
     SpreadParams<R> p = p0;
     const size_t base = spread_smem(p.g, p.ln);
-    const size_t raw = p.s.cr ? 2 * (size_t)(CX ? 2 : 1) * SPREAD_CHUNK_ENTRIES * p.s.jsum * sizeof(R) : 0;
+    const size_t raw = p.s.cr ? (size_t)(CX ? 2 : 1) * SPREAD_CHUNK_ENTRIES * p.s.jsum * sizeof(R) : 0;
     p.cpf = p.s.cr && base + raw <= SPREAD_CPF_SMEM;
     const size_t smem = base + (p.cpf ? raw : 0);
     cudaError_t e = ensure_smem(spread_kernel<R, NDIM, CX, JJ, LSC, ROWSKIP>, smem);
