@@ -68,6 +68,20 @@ def test_geometry_struct_layout_matches_c(tmp_path):
         assert getattr(GbnGeometry, f).offset == off, f
 
 
+def test_header_constants_match_python_mirror():
+    """Status codes, precision / phasing values and geometry flags: every
+    #define of include/gbnufft.h against the constants of _lib.py."""
+    from mrrt.nufft_gb300 import _lib
+
+    defines = dict(re.findall(r"#define\s+(GBN_[A-Z_]+)\s+(\d+)", open(HEADER).read()))
+    mirror = {k: getattr(_lib, k) for k in dir(_lib) if k.startswith("GBN_ERR_") or k == "GBN_OK"}
+    mirror.update({"GBN_FLAG_" + k[5:]: getattr(_lib, k) for k in dir(_lib) if k.startswith("FLAG_")})
+    mirror.update({"GBN_PRECISION_" + k.upper(): v for k, v in _lib.PRECISION.items()})
+    mirror.update({"GBN_PHASING_" + k.upper(): v for k, v in _lib.PHASING.items()})
+    numeric = {k: int(v) for k, v in defines.items() if not k.startswith("GBN_NOALLOC")}
+    assert numeric == mirror
+
+
 def _geom(**kw):
     from mrrt.nufft_gb300._lib import GbnGeometry
 
