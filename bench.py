@@ -351,6 +351,27 @@ def config_dict(extra=None):
     return cfg
 
 
+# FFT lengths the library transforms with its own passes (gbn_colfft.cu,
+# gbn_rowfft.cu); the other lengths use cuFFT (whose launches are not ours)
+OWN_FFT_LENGTHS = (64, 96, 128, 192, 256, 384, 512, 768)
+
+
+def our_launches_per_step(Kd, split_tiles):
+    """Launches of this library's kernels in one forward + adjoint pair of a
+    single-precision plan: with every axis length supported, the row pass
+    (pad or crop folded in), the strided-axis passes and the interpolation
+    kernel each way; else pad / crop and the interpolation kernel, plus the
+    last-axis pass when its length is supported; the reduce of split tiles."""
+    nd = len(Kd)
+    if nd >= 2 and all(k in OWN_FFT_LENGTHS for k in Kd):
+        per_dir = nd + 1
+    elif nd >= 2 and Kd[-1] in OWN_FFT_LENGTHS:
+        per_dir = 3
+    else:
+        per_dir = 2
+    return 2 * per_dir + (1 if split_tiles > 0 else 0)
+
+
 def _clock_path(rank):
     """Where the clock sampler writes: $GBN_BENCH_OUT, else the working directory."""
     out = os.environ.get("GBN_BENCH_OUT", ".")
@@ -427,7 +448,7 @@ def run_ours(args, rank, world):
         parity_gate(parity)
 
     stats = P.stats()
-    launches_per_step = 2 + 2 + (1 if stats["split_tiles"] > 0 else 0)
+    launches_per_step = our_launches_per_step(w["Kd"], stats["split_tiles"])
 
     # ---- batched, device resident: the step replayed from a CUDA graph -----
     for _ in range(args.warmup):
@@ -745,7 +766,7 @@ def run_series(args, rank, world):
         parity_gate(parity)
 
     stats = S.plan.stats()
-    launches_per_step = 2 + 2 + (1 if stats["split_tiles"] > 0 else 0)
+    launches_per_step = our_launches_per_step(w["Kd"], stats["split_tiles"])
 
     # ---- batched series from CUDA graphs, device resident -------------------
     for _ in range(args.warmup):
