@@ -60,3 +60,18 @@ def test_bench_parity_gate():
     for bad in (0.93, 2e-4, float("nan")):
         with pytest.raises(SystemExit):
             bench.parity_gate({"fwd_rel_err_vs_oracle": bad})
+
+
+def test_own_kernel_launch_count_follows_the_fft_path():
+    """gpu_launches: per pair, the row pass, the strided passes and the
+    interpolation kernel each way when every axis length has an own FFT pass;
+    pad / crop around the interpolation kernels (plus the last-axis pass when
+    only its length is supported) otherwise; one reduce when tiles split."""
+    import bench
+
+    assert bench.our_launches_per_step((512, 512), 1) == 7
+    assert bench.our_launches_per_step((256, 256, 256), 1) == 9
+    assert bench.our_launches_per_step((384, 384), 0) == 6
+    assert bench.our_launches_per_step((40, 512), 0) == 6
+    assert bench.our_launches_per_step((512, 1024), 1) == 5
+    assert bench.our_launches_per_step((1024,), 0) == 4
