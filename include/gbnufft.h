@@ -145,12 +145,11 @@ int gbn_adjoint(gbn_plan* plan, const void* y, void* x, int coils,
  * and 454-481).  x and y are host pointers in the layouts above (pageable
  * or pinned); the call copies the input in, transforms on `stream` and
  * returns once the result is in host memory.  Single-frame batches of 32
- * coils or more run as a copy / transform pipeline of 16-coil chunks on two
- * copy streams the plan owns.  Pageable inputs are read in place by a copy
- * kernel where the device reports cudaDevAttrPageableMemoryAccess, else
- * copied by the copy engines; pinned outputs let the copies run at the
- * link's full rate.  Device pointers and calls during graph capture are
- * rejected.                                                                 */
+ * coils or more run as a copy / transform pipeline of 16-coil chunks (the
+ * forward starts with two 8-coil chunks) on two copy streams the plan owns;
+ * every copy, pageable or pinned, runs on the copy engines.  Pinned outputs
+ * let the copies run at the link's full rate.  Device pointers and calls
+ * during graph capture are rejected.                                        */
 int gbn_forward_host(gbn_plan* plan, const void* x_host, void* y_host,
                      int coils, void* stream);
 int gbn_adjoint_host(gbn_plan* plan, const void* y_host, void* x_host,
